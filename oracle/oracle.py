@@ -1,0 +1,110 @@
+"""ctypes loader for the two CPU checkers (test infrastructure only; the product never imports this).
+
+  port()       -> our C++ restatement of the reference path (oracle/sb_oracle.cpp), built by `make port`
+  reference()  -> the reference's own sources compiled here (oracle/_ref/libsbref.so), built by `make ref`;
+                  only available where the reference sources exist (None elsewhere)
+
+Both return a Checker whose run() gives a dict of numpy arrays named as in oracle/sb_oracle.h.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libsb_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsbref.so")
+REF_ROOT = os.environ.get("SB_REFERENCE_ROOT", "/root/reference")
+
+_NAMES_I64 = ["status", "cand", "isect", "newt", "groups_a_off", "groups_a", "groups_b_off", "groups_b",
+              "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"]
+_NAMES_F64 = ["seg", "newv", "time_ms"]
+_SHAPES = {"cand": (-1, 2), "seg": (-1, 6), "newv": (-1, 3), "newt": (-1, 3), "union": (-1, 3),
+           "diff": (-1, 3), "intersect": (-1, 3)}
+
+
+def build(target: str = "port") -> None:
+    subprocess.check_call(["make", "-s", "-C", HERE, target, f"REF_ROOT={REF_ROOT}"])
+
+
+class Checker:
+    def __init__(self, path: str):
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        L.sbo_run.restype = ctypes.c_void_p
+        L.sbo_run.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                              ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                              ctypes.c_long]
+        L.sbo_len.restype = ctypes.c_long
+        L.sbo_len.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.sbo_get_i64.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        L.sbo_get_f64.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        L.sbo_free.argtypes = [ctypes.c_void_p]
+        L.sbo_earcut.restype = ctypes.c_long
+        L.sbo_earcut.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p,
+                                 ctypes.c_long]
+        L.sbo_tritri.restype = ctypes.c_int
+        L.sbo_tritri.argtypes = [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+
+    def run(self, va, fa, vb, fb, quantum: int = 100000) -> dict:
+        va = np.ascontiguousarray(va, dtype=np.float64)
+        vb = np.ascontiguousarray(vb, dtype=np.float64)
+        fa = np.ascontiguousarray(fa, dtype=np.uint32)
+        fb = np.ascontiguousarray(fb, dtype=np.uint32)
+        h = self.lib.sbo_run(va.ctypes.data, len(va), fa.ctypes.data, len(fa),
+                             vb.ctypes.data, len(vb), fb.ctypes.data, len(fb), int(quantum))
+        out = {}
+        try:
+            for names, dt, getter in ((_NAMES_I64, np.int64, self.lib.sbo_get_i64),
+                                      (_NAMES_F64, np.float64, self.lib.sbo_get_f64)):
+                for n in names:
+                    ln = self.lib.sbo_len(h, n.encode())
+                    if ln < 0:
+                        continue
+                    arr = np.zeros(ln, dtype=dt)
+                    getter(h, n.encode(), arr.ctypes.data)
+                    out[n] = arr.reshape(_SHAPES[n]) if n in _SHAPES else arr
+        finally:
+            self.lib.sbo_free(h)
+        out["status"] = int(out["status"][0])
+        return out
+
+    def earcut(self, rings) -> np.ndarray:
+        xy = np.ascontiguousarray(np.concatenate([np.asarray(r, dtype=np.float64).reshape(-1, 2)
+                                                  for r in rings]))
+        off = np.zeros(len(rings) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(r) for r in rings])
+        cap = max(16, 3 * 3 * len(xy))
+        out = np.zeros(cap, dtype=np.int64)
+        n = self.lib.sbo_earcut(xy.ctypes.data, off.ctypes.data, len(rings), out.ctypes.data, cap)
+        assert n <= cap
+        return out[:n].copy()
+
+    def tritri(self, p1, q1, r1, p2, q2, r2):
+        args = [np.ascontiguousarray(x, dtype=np.float64) for x in (p1, q1, r1, p2, q2, r2)]
+        cop = ctypes.c_int(0)
+        seg = np.zeros(6)
+        r = self.lib.sbo_tritri(*[a.ctypes.data for a in args], ctypes.byref(cop), seg.ctypes.data)
+        return r, cop.value, seg
+
+
+_cache: dict[str, Checker] = {}
+
+
+def port() -> Checker:
+    if "port" not in _cache:
+        build("port")
+        _cache["port"] = Checker(PORT_SO)
+    return _cache["port"]
+
+
+def reference() -> Checker | None:
+    if "ref" not in _cache:
+        if not os.path.isdir(os.path.join(REF_ROOT, "src")):
+            return None
+        build("ref")
+        _cache["ref"] = Checker(REF_SO)
+    return _cache["ref"]
