@@ -1,0 +1,119 @@
+/*
+ * solidboolean_gb300 — C ABI of the GB300 mesh-boolean path.
+ *
+ * Drop-in for the reference's call sequence (huxingyi/solidboolean):
+ *
+ *   reference (C++)                                         this library
+ *   SolidMesh m; m.setVertices(&v); m.setTriangles(&t);     sb_mesh_create(xyz, nv, tris, nt, &m)
+ *     (src/solidmesh.h:33-34, src/solidmesh.cpp:32-40)
+ *   m.prepare()            (src/solidmesh.cpp:42-76)        sb_mesh_prepare(m, &opts)
+ *   SolidBoolean b(&m1, &m2) (src/solidboolean.h:36-37)     sb_boolean_create(m1, m2, &opts, &b)
+ *   bool ok = b.combine()  (src/solidboolean.cpp:288-480)   sb_combine(b, &stats) == SB_OK
+ *   b.fetchUnion(tris)     (src/solidboolean.cpp:512-527)   sb_fetch(b, SB_UNION, ...)
+ *   b.fetchDiff(tris)      (src/solidboolean.cpp:529-548)   sb_fetch(b, SB_DIFF, ...)
+ *   b.fetchIntersect(tris) (src/solidboolean.cpp:550-565)   sb_fetch(b, SB_INTERSECT, ...)
+ *   b.resultVertices()     (src/solidboolean.cpp:567-570)   sb_result_vertices(b, ...)
+ *
+ * Every call returns an sb_status; no exception crosses the ABI. Handles own their device memory until
+ * the matching *_destroy. A handle is not thread-safe; distinct handles are independent. Work is ordered
+ * on the stream given in sb_options (0 = the legacy default stream); functions that return host data
+ * synchronise that stream.
+ */
+#ifndef SOLIDBOOLEAN_GB300_H
+#define SOLIDBOOLEAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sb_mesh sb_mesh;
+typedef struct sb_boolean sb_boolean;
+
+typedef enum sb_status {
+    SB_OK = 0,
+    /* combine() returned false in the reference (src/solidboolean.cpp:368-370, 427-445) */
+    SB_FAIL_ATTACH = 1,      /* "Attach point to triangle edge failed" (src/retriangulator.cpp:149-152) */
+    SB_FAIL_LINK = 2,        /* "linkTo failed" (src/retriangulator.cpp:227-229) */
+    SB_FAIL_LOOP = 3,        /* cut edges do not form closed loops (src/solidboolean.cpp:150-158) */
+    /* library errors */
+    SB_ERR_INVALID = 10,     /* bad argument, index out of range, call out of order */
+    SB_ERR_CUDA = 11,        /* a CUDA runtime call failed; see sb_last_error() */
+    SB_ERR_CAPACITY = 12,    /* a per-face scratch bound was exceeded (never expected; reported, not hidden) */
+    SB_ERR_NOT_COMBINED = 13 /* fetch before a successful combine */
+} sb_status;
+
+typedef enum sb_op { SB_UNION = 0, SB_DIFF = 1, SB_INTERSECT = 2 } sb_op;
+
+/* Arithmetic of the orientation predicates and box tests. Both give identical results. */
+typedef enum sb_precision {
+    SB_PRECISION_FILTERED = 0, /* FP32 with static forward-error bounds; FP64 only where not certified */
+    SB_PRECISION_FP64 = 1      /* plain FP64 everywhere */
+} sb_precision;
+
+/* How the pairs of one cut face are ordered before its cut points are numbered. */
+typedef enum sb_order {
+    SB_ORDER_REFERENCE = 0, /* the reference's order (its AABB tree's leaf order), for bit-exact output */
+    SB_ORDER_INDEX = 1      /* ascending triangle index (skips building the reference leaf order) */
+} sb_order;
+
+typedef struct sb_options {
+    int64_t weld_factor; /* PositionKey quantisation factor; the reference uses 100000 (src/positionkey.cpp:25) */
+    int32_t precision;   /* sb_precision */
+    int32_t order;       /* sb_order */
+    void *stream;        /* cudaStream_t */
+} sb_options;
+
+typedef struct sb_stats {
+    uint64_t candidate_pairs;    /* AABB-overlapping triangle pairs */
+    uint64_t intersecting_pairs; /* non-coplanar intersecting pairs */
+    uint64_t cut_faces_first, cut_faces_second;
+    uint64_t new_points;         /* welded cut points appended after the input vertices */
+    uint64_t result_vertices, result_triangles; /* arrangement sizes */
+    uint64_t sign_tests;         /* orientation signs decided (filtered form) */
+    uint64_t sign_fallbacks;     /* of those, re-evaluated in FP64 */
+    uint64_t box_tests, box_fallbacks; /* leaf box tests and FP64 re-tests */
+    uint32_t regions_first, regions_second;
+    uint32_t failed_faces;       /* cut faces whose re-triangulation failed */
+    uint32_t loop_vertices;      /* vertices of the cut loops */
+    uint32_t loop_bad_degree;    /* loop vertices whose degree is not 2 */
+    uint32_t duplicate_halfedges;
+    double stage_ms[8];          /* broad, narrow, faces, weld, assemble, groups, sides, fetch (device time) */
+} sb_stats;
+
+void sb_default_options(sb_options *opts);
+const char *sb_status_string(sb_status s);
+const char *sb_last_error(void);
+
+/* Mesh: vertices are FP64 xyz triplets, triangles are uint32 index triplets. The host variant copies
+ * the arrays; the device variant copies from device pointers on opts->stream. */
+sb_status sb_mesh_create(const double *xyz, size_t nv, const uint32_t *tris, size_t nt, sb_mesh **out);
+sb_status sb_mesh_create_device(const double *d_xyz, size_t nv, const uint32_t *d_tris, size_t nt,
+                                const sb_options *opts, sb_mesh **out);
+/* Replace the vertex positions (same count, device pointer) without rebuilding the handle. */
+sb_status sb_mesh_update_vertices_device(sb_mesh *m, const double *d_xyz, const sb_options *opts);
+sb_status sb_mesh_prepare(sb_mesh *m, const sb_options *opts);
+void sb_mesh_destroy(sb_mesh *m);
+
+sb_status sb_boolean_create(const sb_mesh *first, const sb_mesh *second, const sb_options *opts,
+                            sb_boolean **out);
+sb_status sb_combine(sb_boolean *b, sb_stats *stats);
+/* Host results. Pass tris == NULL to query the count; cap is in triangles / vertices. */
+sb_status sb_fetch(sb_boolean *b, sb_op op, uint32_t *tris, size_t cap, size_t *count);
+sb_status sb_result_vertices(sb_boolean *b, double *xyz, size_t cap, size_t *count);
+/* Device results: pointers stay valid until the next combine or destroy; counts are host values. */
+sb_status sb_fetch_device(sb_boolean *b, sb_op op, const uint32_t **d_tris, size_t *count);
+sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t *count);
+/* Stage dumps for parity checks (host copies). Names: "candidates" (uint32 pairs), "intersections"
+ * (uint32 pair + 6 doubles as raw bytes), "arrangement" (uint32 triangles), "labels" (int8 per arrangement
+ * triangle: 0 outside, 1 inside, -1 ungrouped), "first_range" (uint32 start/count of the first mesh's
+ * triangles in the arrangement). *bytes receives the size; out may be NULL. */
+sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
+void sb_boolean_destroy(sb_boolean *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,610 @@
+// Assembly of the combined arrangement and the inside/outside labelling.
+//
+//   global weld       addNewPoint (src/solidboolean.cpp:241-248): cut points of all faces, first mesh's faces
+//                     first, keyed by PositionKey in a device hash table; the first occurrence in that order
+//                     keeps its coordinates and the new vertices are numbered in first-occurrence order
+//   arrangement       addUnintersectedTriangles (:250-286) and the reTriangulate lambda (:352-407): uncut
+//                     triangles of each mesh (index order) and the re-triangulated faces, with their
+//                     half-edges in per-mesh device hash tables (first owner wins)
+//   cut loops         buildPolygonsFromEdges (:124-165): every loop vertex must have exactly two neighbours
+//   face groups       buildFaceGroups (:167-239): the flood fill crosses every half-edge that is not a cut
+//                     edge and has a twin; its connected components are found with a lock-free union-find
+//   sides             decideGroupSide / isPointInMesh (:482-510, 48-92): three axis rays from the centroid
+//                     of each region's representative triangle, hit points deduplicated by PositionKey,
+//                     inside when at least two of the three parities are odd
+#include <cub/cub.cuh>
+
+#include "sb_assemble.cuh"
+#include "sb_common.cuh"
+
+namespace sbg {
+
+// ---------------------------------------------------------------------------------------------------
+// hash tables (open addressing, linear probing, power-of-two capacity)
+// ---------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t slot_of(uint64_t h, uint32_t mask) { return (uint32_t)(mix64(h) & mask); }
+
+// map uint64 key -> min(int value)
+__device__ void u64map_insert_min(uint64_t *keys, int *vals, uint32_t mask, uint64_t key, int val)
+{
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        uint64_t prev = atomicCAS((unsigned long long *)(keys + s), (unsigned long long)kEmpty64,
+                                  (unsigned long long)key);
+        if (prev == kEmpty64 || prev == key) {
+            atomicMin(vals + s, val);
+            return;
+        }
+        s = (s + 1) & mask;
+    }
+}
+__device__ int u64map_find(const uint64_t *keys, const int *vals, uint32_t mask, uint64_t key)
+{
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        uint64_t k = keys[s];
+        if (k == key)
+            return vals[s];
+        if (k == kEmpty64)
+            return -1;
+        s = (s + 1) & mask;
+    }
+    return -1;
+}
+
+// ---- global weld ------------------------------------------------------------------------------------
+// seq = position of a cut point in (face order, local order); slots claim by the first seq to arrive and
+// keep the minimum seq of the key
+__global__ void k_weld_insert(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ faceNpts,
+                              const Key *__restrict__ keys, int *slotOwner, int *slotMin, uint32_t mask,
+                              int *pointSlot)
+{
+    int f = blockIdx.x;
+    if (f >= nFaces)
+        return;
+    int n = faceNpts[f];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int seq = ptOff[f] + k;
+        Key key = keys[seq];
+        uint32_t s = (uint32_t)(key_hash(key) & mask);
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            int o = atomicCAS(slotOwner + s, -1, seq);
+            if (o == -1 || key_eq(keys[o], key)) {
+                atomicMin(slotMin + s, seq);
+                pointSlot[seq] = (int)s;
+                break;
+            }
+            s = (s + 1) & mask;
+        }
+    }
+}
+
+// first occurrences flagged per seq position
+__global__ void k_weld_first(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ faceNpts,
+                             const int *__restrict__ pointSlot, const int *__restrict__ slotMin, int *isFirst)
+{
+    int f = blockIdx.x;
+    if (f >= nFaces)
+        return;
+    int n = faceNpts[f];
+    for (int k = threadIdx.x; k < ptOff[f + 1] - ptOff[f]; k += blockDim.x) {
+        int seq = ptOff[f] + k;
+        isFirst[seq] = (k < n && slotMin[pointSlot[seq]] == seq) ? 1 : 0;
+    }
+}
+
+__global__ void k_weld_number(int nSeq, const int *__restrict__ isFirst, const int *__restrict__ firstRank,
+                              const int *__restrict__ pointSlot, int *slotRank, const d3 *__restrict__ pts,
+                              double *newV, int vbase)
+{
+    int seq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seq >= nSeq || !isFirst[seq])
+        return;
+    int r = firstRank[seq];
+    slotRank[pointSlot[seq]] = r;
+    d3 p = pts[seq];
+    double *o = newV + 3 * (size_t)(vbase + r);
+    o[0] = p.x;
+    o[1] = p.y;
+    o[2] = p.z;
+}
+
+// ---- arrangement ------------------------------------------------------------------------------------
+__global__ void k_mark_cut(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ faceTri,
+                           int *cutA, int *cutB)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nFaces)
+        return;
+    if (faceSide[f] == 0)
+        cutA[faceTri[f]] = 1;
+    else
+        cutB[faceTri[f]] = 1;
+}
+
+// uncut triangles of one mesh, in index order, offset into the arrangement
+__global__ void k_uncut(int nt, const uint32_t *__restrict__ t, const int *__restrict__ cut,
+                        const int *__restrict__ uncutRank, uint32_t vbase, uint32_t outBase, uint32_t *newT)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt || cut[i])
+        return;
+    uint32_t o = outBase + (uint32_t)uncutRank[i];
+    newT[3 * (size_t)o] = t[3 * (size_t)i] + vbase;
+    newT[3 * (size_t)o + 1] = t[3 * (size_t)i + 1] + vbase;
+    newT[3 * (size_t)o + 2] = t[3 * (size_t)i + 2] + vbase;
+}
+
+__device__ __forceinline__ uint32_t local_to_global(int local, const uint32_t *tri, uint32_t vbase, int ptBase,
+                                                   const int *pointSlot, const int *slotRank, uint32_t newBase)
+{
+    if (local < 3)
+        return tri[local] + vbase;
+    return newBase + (uint32_t)slotRank[pointSlot[ptBase + local - 3]];
+}
+
+__global__ void k_retri(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ faceTri,
+                        const int *__restrict__ faceNtris, const int *__restrict__ triOff,
+                        const int *__restrict__ retriRank, const int *__restrict__ faceTris,
+                        const int *__restrict__ ptOff, const int *__restrict__ pointSlot,
+                        const int *__restrict__ slotRank, MeshDev A, MeshDev B, uint32_t newBase, uint32_t outBase,
+                        uint32_t *newT)
+{
+    int f = blockIdx.x;
+    if (f >= nFaces)
+        return;
+    const MeshDev &M = faceSide[f] == 0 ? A : B;
+    uint32_t vbase = faceSide[f] == 0 ? 0u : (uint32_t)A.nv;
+    const uint32_t *tri = M.t + 3 * (size_t)faceTri[f];
+    int n = faceNtris[f];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int *lt = faceTris + 3 * (size_t)(triOff[f] + k);
+        uint32_t o = outBase + (uint32_t)(retriRank[f] + k);
+        for (int c = 0; c < 3; ++c)
+            newT[3 * (size_t)o + c] = local_to_global(lt[c], tri, vbase, ptOff[f], pointSlot, slotRank, newBase);
+    }
+}
+
+// ---- cut loops (first mesh's cut edges) ----------------------------------------------------------------
+__global__ void k_cut_edges(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ faceNedges,
+                            const int *__restrict__ edgeOff, const int *__restrict__ faceEdges,
+                            const int *__restrict__ ptOff, const int *__restrict__ pointSlot,
+                            const int *__restrict__ slotRank, uint64_t *edgeKeys, int *edgeVals, uint32_t mask,
+                            int sideWanted)
+{
+    int f = blockIdx.x;
+    if (f >= nFaces || faceSide[f] != sideWanted)
+        return;
+    for (int k = threadIdx.x; k < faceNedges[f]; k += blockDim.x) {
+        const int *e = faceEdges + 2 * (size_t)(edgeOff[f] + k);
+        uint32_t u = (uint32_t)slotRank[pointSlot[ptOff[f] + e[0] - 3]];
+        uint32_t v = (uint32_t)slotRank[pointSlot[ptOff[f] + e[1] - 3]];
+        if (u == v)
+            continue;
+        uint32_t lo = min(u, v), hi = max(u, v);
+        u64map_insert_min(edgeKeys, edgeVals, mask, ((uint64_t)lo << 32) | hi, 0);
+    }
+}
+
+__global__ void k_loop_degree(uint32_t cap, const uint64_t *__restrict__ edgeKeys, int *degree)
+{
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cap)
+        return;
+    uint64_t k = edgeKeys[s];
+    if (k == kEmpty64)
+        return;
+    atomicAdd(degree + (uint32_t)(k >> 32), 1);
+    atomicAdd(degree + (uint32_t)(k & 0xFFFFFFFFu), 1);
+}
+
+__global__ void k_loop_check(int n, const int *__restrict__ degree, unsigned int *counters)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int d = degree[i];
+    if (d > 0)
+        atomicAdd(counters + 0, 1u);
+    if (d > 0 && d != 2)
+        atomicAdd(counters + 1, 1u);
+}
+
+// ---- half-edge tables, union-find ---------------------------------------------------------------------
+__device__ __forceinline__ uint64_t he_key(uint32_t a, uint32_t b) { return ((uint64_t)a << 32) | b; }
+
+__global__ void k_halfedges(int nTri, const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh,
+                            uint64_t *keysA, int *valsA, uint64_t *keysB, int *valsB, uint32_t mask)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    const uint32_t *v = newT + 3 * (size_t)t;
+    uint64_t *keys = triMesh[t] == 0 ? keysA : keysB;
+    int *vals = triMesh[t] == 0 ? valsA : valsB;
+    for (int i = 0; i < 3; ++i)
+        u64map_insert_min(keys, vals, mask, he_key(v[i], v[(i + 1) % 3]), t);
+}
+
+__device__ __forceinline__ bool is_cut_edge(const uint64_t *edgeKeys, const int *edgeVals, uint32_t emask, uint32_t u,
+                                            uint32_t v, uint32_t newBase)
+{
+    if (u < newBase || v < newBase)
+        return false;
+    uint32_t a = u - newBase, b = v - newBase;
+    uint32_t lo = min(a, b), hi = max(a, b);
+    return u64map_find(edgeKeys, edgeVals, emask, ((uint64_t)lo << 32) | hi) >= 0;
+}
+
+__device__ int uf_find(int *parent, int x)
+{
+    while (true) {
+        int p = parent[x];
+        if (p == x)
+            return x;
+        int gp = parent[p];
+        if (gp != p)
+            atomicCAS(parent + x, p, gp); // path halving
+        x = gp;
+    }
+}
+
+__device__ void uf_union(int *parent, int a, int b)
+{
+    while (true) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b)
+            return;
+        if (a < b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        if (atomicCAS(parent + a, a, b) == a)
+            return;
+    }
+}
+
+__global__ void k_union(int nTri, const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh,
+                        const uint64_t *keysA, const int *valsA, const uint64_t *keysB, const int *valsB,
+                        uint32_t mask, const uint64_t *edgeKeys, const int *edgeVals, uint32_t emask,
+                        uint32_t newBase, int *parent, int *seedFlag, unsigned int *dupCount)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    const uint32_t *v = newT + 3 * (size_t)t;
+    const uint64_t *keys = triMesh[t] == 0 ? keysA : keysB;
+    const int *vals = triMesh[t] == 0 ? valsA : valsB;
+    int seed = 0;
+    for (int i = 0; i < 3; ++i) {
+        uint32_t a = v[i], b = v[(i + 1) % 3];
+        int owner = u64map_find(keys, vals, mask, he_key(a, b));
+        if (owner != t)
+            atomicAdd(dupCount, 1u);
+        if (is_cut_edge(edgeKeys, edgeVals, emask, a, b, newBase)) {
+            if (owner == t)
+                seed = 1;
+            continue;
+        }
+        if (owner != t)
+            continue; // a repeated half-edge was already crossed by its first owner
+        int tw = u64map_find(keys, vals, mask, he_key(b, a));
+        if (tw >= 0)
+            uf_union(parent, t, tw);
+    }
+    seedFlag[t] = seed;
+}
+
+__global__ void k_uf_flatten(int n, int *parent)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n)
+        return;
+    parent[t] = uf_find(parent, t);
+}
+
+// representative triangle of each region: the smallest seed triangle, else the smallest uncut triangle
+__global__ void k_region_rep(int nTri, const int *__restrict__ root, const int *__restrict__ seedFlag,
+                             const int8_t *__restrict__ isUncut, int *seedMin, int *remMin)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    int r = root[t];
+    if (seedFlag[t])
+        atomicMin(seedMin + r, t);
+    if (isUncut[t])
+        atomicMin(remMin + r, t);
+}
+
+__global__ void k_region_list(int nTri, const int *__restrict__ root, const int *__restrict__ seedMin,
+                              const int *__restrict__ remMin, int *repOfRoot, int *reps, unsigned int *nReps,
+                              const int8_t *__restrict__ triMesh, unsigned int *regionsPerMesh)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri || root[t] != t)
+        return;
+    int rep = seedMin[t] != INT_MAX ? seedMin[t] : (remMin[t] != INT_MAX ? remMin[t] : -1);
+    repOfRoot[t] = rep;
+    if (rep >= 0) {
+        unsigned int k = atomicAdd(nReps, 1u);
+        reps[k] = t;
+        atomicAdd(regionsPerMesh + triMesh[t], 1u);
+    }
+}
+
+// isPointInMesh (src/solidboolean.cpp:48-92) for one (region, axis)
+template <bool FP64>
+__global__ void k_sides(unsigned int nReps, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
+                        const uint32_t *__restrict__ newT, const double *__restrict__ newV,
+                        const int8_t *__restrict__ triMesh, MeshDev A, MeshDev B, double factor, int *insideCount,
+                        unsigned int *errors)
+{
+    unsigned int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= 3 * nReps)
+        return;
+    int r = reps[w / 3];
+    int axis = (int)(w % 3);
+    int rep = repOfRoot[r];
+    const MeshDev &M = triMesh[rep] == 0 ? B : A; // the other mesh
+    const uint32_t *tv = newT + 3 * (size_t)rep;
+    d3 v0 = mk(newV[3 * (size_t)tv[0]], newV[3 * (size_t)tv[0] + 1], newV[3 * (size_t)tv[0] + 2]);
+    d3 v1 = mk(newV[3 * (size_t)tv[1]], newV[3 * (size_t)tv[1] + 1], newV[3 * (size_t)tv[1] + 2]);
+    d3 v2 = mk(newV[3 * (size_t)tv[2]], newV[3 * (size_t)tv[2] + 1], newV[3 * (size_t)tv[2] + 2]);
+    d3 p = divs((v0 + v1) + v2, 3.0);
+    d3 ax = mk(axis == 0 ? kDblMax : kDblEps, axis == 1 ? kDblMax : kDblEps, axis == 2 ? kDblMax : kDblEps);
+    d3 e = p + ax;
+    double qlo[3], qhi[3];
+    for (int k = 0; k < 3; ++k) {
+        double a = comp(p, k), b = comp(e, k);
+        // AxisAlignedBoudingBox::update with p then e
+        double lo = kDblMax, hi = -kDblMax;
+        if (a > hi)
+            hi = a;
+        if (a < lo)
+            lo = a;
+        if (b > hi)
+            hi = b;
+        if (b < lo)
+            lo = b;
+        qlo[k] = lo;
+        qhi[k] = hi;
+    }
+    float olo[3], ohi[3];
+    for (int k = 0; k < 3; ++k) {
+        olo[k] = __double2float_rd(qlo[k]);
+        ohi[k] = __double2float_ru(qhi[k]);
+    }
+    Key hits[64];
+    int nh = 0;
+    bool overflow = false;
+    d3 u = e - p;
+    auto test_tri = [&](int ti) {
+        const double *bx = M.box64 + 6 * (size_t)ti;
+        for (int k = 0; k < 3; ++k)
+            if (!(bx[k] <= qhi[k] && bx[3 + k] >= qlo[k]))
+                return;
+        const uint32_t *t = M.t + 3 * (size_t)ti;
+        d3 tp[3];
+        for (int k = 0; k < 3; ++k)
+            tp[k] = mk(M.v[3 * (size_t)t[k]], M.v[3 * (size_t)t[k] + 1], M.v[3 * (size_t)t[k] + 2]);
+        d3 n = unit_normal(tp[0], tp[1], tp[2]);
+        d3 wv = p - tp[0];
+        double d = dot(n, u);
+        double nn = dot(neg(n), wv);
+        if (fabs(d) <= kDblEps)
+            return;
+        double s = nn / d;
+        if (s < 0 || s > 1 || isnan(s) || isinf(s))
+            return;
+        d3 x = p + scale(s, u);
+        d3 n0 = unit_normal(x, tp[0], tp[1]);
+        d3 n1 = unit_normal(x, tp[1], tp[2]);
+        d3 n2 = unit_normal(x, tp[2], tp[0]);
+        if (!(dot(n0, n1) > 0 && dot(n0, n2) > 0))
+            return;
+        Key k = make_key(x, factor);
+        for (int q = 0; q < nh; ++q)
+            if (key_eq(hits[q], k))
+                return;
+        if (nh < 64)
+            hits[nh++] = k;
+        else
+            overflow = true;
+    };
+    if (M.nt > 0) {
+        if (M.root < 0) {
+            test_tri(M.leafTri[0]);
+        } else {
+            int stack[96];
+            int sp = 0;
+            stack[sp++] = M.root;
+            while (sp > 0) {
+                int node = stack[--sp];
+                int2 ch = M.child[node];
+                int cs[2] = {ch.x, ch.y};
+                for (int k = 0; k < 2; ++k) {
+                    int c = cs[k];
+                    if (c < 0) {
+                        test_tri(M.leafTri[~c]);
+                        continue;
+                    }
+                    bool hit;
+                    if (FP64) {
+                        const double *bx = M.nbox64 + 6 * (size_t)c;
+                        hit = qlo[0] <= bx[3] && qhi[0] >= bx[0] && qlo[1] <= bx[4] && qhi[1] >= bx[1] &&
+                              qlo[2] <= bx[5] && qhi[2] >= bx[2];
+                    } else {
+                        const float *bx = M.nbox32 + 6 * (size_t)c;
+                        hit = olo[0] <= bx[3] && ohi[0] >= bx[0] && olo[1] <= bx[4] && ohi[1] >= bx[1] &&
+                              olo[2] <= bx[5] && ohi[2] >= bx[2];
+                    }
+                    if (hit) {
+                        if (sp < 96)
+                            stack[sp++] = c;
+                        else
+                            overflow = true;
+                    }
+                }
+            }
+        }
+    }
+    if (overflow)
+        atomicAdd(errors, 1u);
+    if (nh % 2 != 0)
+        atomicAdd(insideCount + r, 1);
+}
+
+__global__ void k_labels(int nTri, const int *__restrict__ root, const int *__restrict__ repOfRoot,
+                         const int *__restrict__ insideCount, int8_t *label)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    int r = root[t];
+    if (repOfRoot[r] < 0) {
+        label[t] = -1;
+        return;
+    }
+    // (float)insideCount / 3 > 0.5
+    label[t] = ((float)insideCount[r] / 3.0f > 0.5f) ? 1 : 0;
+}
+
+// fetch flags: union keeps outside of both, intersect inside of both, diff outside of the first and
+// inside of the second (reversed) (src/solidboolean.cpp:512-565)
+__global__ void k_fetch_flags(int nTri, const int8_t *__restrict__ label, const int8_t *__restrict__ triMesh,
+                              int op, int *flag)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    int l = label[t];
+    int keep;
+    if (l < 0)
+        keep = 0;
+    else if (op == 0)
+        keep = l == 0;
+    else if (op == 2)
+        keep = l == 1;
+    else
+        keep = triMesh[t] == 0 ? (l == 0) : (l == 1);
+    flag[t] = keep;
+}
+
+__global__ void k_fetch_write(int nTri, const int *__restrict__ flag, const int *__restrict__ rank,
+                              const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh, int op,
+                              uint32_t *out)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri || !flag[t])
+        return;
+    const uint32_t *v = newT + 3 * (size_t)t;
+    uint32_t *o = out + 3 * (size_t)rank[t];
+    if (op == 1 && triMesh[t] == 1) {
+        o[0] = v[2];
+        o[1] = v[1];
+        o[2] = v[0];
+    } else {
+        o[0] = v[0];
+        o[1] = v[1];
+        o[2] = v[2];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------------------------------
+static inline int nb(size_t n, int bs) { return (int)((n + bs - 1) / bs); }
+
+void launch_weld(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.nFaces <= 0)
+        return;
+    k_weld_insert<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.cutKeys, g.weldOwner, g.weldMin,
+                                          g.weldMask, g.pointSlot);
+    k_weld_first<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.pointSlot, g.weldMin, g.isFirst);
+}
+
+void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s)
+{
+    if (nSeq <= 0)
+        return;
+    k_weld_number<<<nb(nSeq, 256), 256, 0, s>>>(nSeq, g.isFirst, g.firstRank, g.pointSlot, g.slotRank, g.cutPts,
+                                                g.newV, g.newBase);
+}
+
+void launch_mark_cut(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.nFaces > 0)
+        k_mark_cut<<<nb(g.nFaces, 256), 256, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.cutA, g.cutB);
+}
+
+void launch_arrangement(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.A.nt > 0)
+        k_uncut<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT);
+    if (g.B.nt > 0)
+        k_uncut<<<nb(g.B.nt, 256), 256, 0, s>>>(g.B.nt, g.B.t, g.cutB, g.uncutRankB, (uint32_t)g.A.nv,
+                                                (uint32_t)g.uncutA, g.newT);
+    if (g.nFaces > 0)
+        k_retri<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.faceNtris, g.triOff, g.retriRank,
+                                        g.faceTris, g.ptOff, g.pointSlot, g.slotRank, g.A, g.B,
+                                        (uint32_t)g.newBase, (uint32_t)(g.uncutA + g.uncutB), g.newT);
+}
+
+void launch_loops(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.nFaces > 0)
+        k_cut_edges<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceNedges, g.edgeOff, g.faceEdges, g.ptOff,
+                                            g.pointSlot, g.slotRank, g.edgeKeys, g.edgeVals, g.edgeMask, 0);
+    k_loop_degree<<<nb((size_t)g.edgeMask + 1, 256), 256, 0, s>>>(g.edgeMask + 1, g.edgeKeys, g.degree);
+    if (g.nNew > 0)
+        k_loop_check<<<nb(g.nNew, 256), 256, 0, s>>>(g.nNew, g.degree, g.counters + kCntLoopVerts);
+}
+
+void launch_groups(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.nTri <= 0)
+        return;
+    k_halfedges<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
+                                                g.heValsB, g.heMask);
+    k_union<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
+                                            g.heMask, g.edgeKeys, g.edgeVals, g.edgeMask, (uint32_t)g.newBase,
+                                            g.parent, g.seedFlag, g.counters + kCntDupHalfedge);
+    k_uf_flatten<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent);
+    k_region_rep<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedFlag, g.isUncut, g.seedMin, g.remMin);
+    k_region_list<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot, g.reps,
+                                                  g.counters + kCntReps, g.triMesh, g.counters + kCntRegionsA);
+}
+
+void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s)
+{
+    if (nReps > 0) {
+        if (fp64)
+            k_sides<true><<<nb(3 * (size_t)nReps, 64), 64, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
+                                                                   g.triMesh, g.A, g.B, g.factor, g.insideCount,
+                                                                   g.counters + kCntSideErrors);
+        else
+            k_sides<false><<<nb(3 * (size_t)nReps, 64), 64, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
+                                                                    g.triMesh, g.A, g.B, g.factor, g.insideCount,
+                                                                    g.counters + kCntSideErrors);
+    }
+    if (g.nTri > 0)
+        k_labels<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.repOfRoot, g.insideCount, g.label);
+}
+
+void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s)
+{
+    if (g.nTri > 0)
+        k_fetch_flags<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.label, g.triMesh, op, flag);
+}
+
+void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s)
+{
+    if (g.nTri > 0)
+        k_fetch_write<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, flag, rank, g.newT, g.triMesh, op, out);
+}
+
+} // namespace sbg

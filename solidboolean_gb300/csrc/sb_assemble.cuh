@@ -1,0 +1,67 @@
+// Assembly / labelling launch interface.
+#pragma once
+#include "sb_common.cuh"
+#include "sb_internal.h"
+
+namespace sbg {
+
+constexpr uint64_t kEmpty64 = ~0ull;
+
+// device counters (unsigned int) used by the assembly kernels
+enum {
+    kCntLoopVerts = 0,   // [0] loop vertices, [1] loop vertices with degree != 2
+    kCntDupHalfedge = 2, // triangles' half-edges whose table owner is another triangle
+    kCntReps = 3,        // number of regions with a representative
+    kCntRegionsA = 4,    // [4] first mesh, [5] second mesh
+    kCntSideErrors = 6,  // hit-buffer or stack overflow in the side rays
+    kCntCount = 8
+};
+
+struct AsmArgs {
+    MeshDev A, B;
+    double factor;
+    int nFaces;
+    const int *faceSide, *faceTri, *faceNpts, *faceNtris, *faceNedges;
+    const int *ptOff, *triOff, *edgeOff;
+    const d3 *cutPts;
+    const Key *cutKeys;
+    const int *faceTris, *faceEdges;
+    // weld
+    int *weldOwner, *weldMin;
+    uint32_t weldMask;
+    int *pointSlot, *isFirst, *firstRank, *slotRank;
+    int newBase; // = A.nv + B.nv
+    int nNew;    // unique cut points
+    double *newV;
+    // arrangement
+    int *cutA, *cutB, *uncutRankA, *uncutRankB;
+    int uncutA, uncutB;
+    const int *retriRank; // per face: offset of its triangles within the re-triangulated block
+    uint32_t *newT;
+    int nTri;
+    int8_t *triMesh, *isUncut;
+    // loops
+    uint64_t *edgeKeys;
+    int *edgeVals;
+    uint32_t edgeMask;
+    int *degree;
+    // groups
+    uint64_t *heKeysA, *heKeysB;
+    int *heValsA, *heValsB;
+    uint32_t heMask;
+    int *parent, *seedFlag, *seedMin, *remMin, *repOfRoot, *reps, *insideCount;
+    int8_t *label;
+    unsigned int *counters;
+};
+
+void launch_weld(const AsmArgs &g, cudaStream_t s);
+void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s);
+void launch_mark_cut(const AsmArgs &g, cudaStream_t s);
+void launch_arrangement(const AsmArgs &g, cudaStream_t s);
+void launch_loops(const AsmArgs &g, cudaStream_t s);
+void launch_groups(const AsmArgs &g, cudaStream_t s);
+void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s);
+void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s);
+void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s);
+
+} // namespace sbg

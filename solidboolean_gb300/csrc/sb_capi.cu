@@ -1,0 +1,1105 @@
+// C ABI and host orchestration of the GB300 boolean (see include/solidboolean_gb300.h).
+//
+// combine() is the reference's SolidBoolean::combine (src/solidboolean.cpp:288-480) as a sequence of
+// device stages on one stream: broad phase, narrow phase, per-face re-triangulation, global weld,
+// arrangement, cut-loop check, union-find regions, side rays, fetch compaction. The host only reads the
+// handful of counts that size the next stage (candidates, intersecting pairs, faces, per-face totals).
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include "sb_assemble.cuh"
+#include "sb_common.cuh"
+#include "sb_faces.cuh"
+#include "sb_internal.h"
+#include "sb_pairs.cuh"
+
+namespace sbg {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+sb_status cuda_fail(cudaError_t e, const char *expr, const char *file, int line)
+{
+    set_last_error(std::string(cudaGetErrorString(e)) + " in " + expr + " (" + file + ":" + std::to_string(line) +
+                   ")");
+    return SB_ERR_CUDA;
+}
+
+cudaError_t DevBuf::ensure(size_t need)
+{
+    if (need <= bytes && ptr)
+        return cudaSuccess;
+    release();
+    size_t n = std::max<size_t>(need + need / 4, 1024);
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        return e;
+    }
+    bytes = n;
+    return cudaSuccess;
+}
+
+void DevBuf::release()
+{
+    if (ptr)
+        cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+static size_t mesh_bytes(int nv, int nt)
+{
+    Carve c;
+    c.take<double>((size_t)nv * 3);
+    c.take<uint32_t>((size_t)nt * 3);
+    c.take<float4>((size_t)nv);
+    c.take<double>((size_t)nt * 6);
+    c.take<float>((size_t)nt * 6);
+    c.take<uint32_t>((size_t)nt);
+    c.take<int>((size_t)nt);
+    c.take<int2>((size_t)(nt > 1 ? nt - 1 : 1));
+    c.take<int>((size_t)(2 * nt));
+    c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
+    c.take<int>((size_t)nt);
+    return c.off;
+}
+
+static uint32_t pow2_at_least(size_t n)
+{
+    uint32_t p = 1024;
+    while (p < n)
+        p <<= 1;
+    return p;
+}
+
+static inline int blocks(size_t n, int bs) { return (int)((n + bs - 1) / bs); }
+
+// ---- small helper kernels ---------------------------------------------------------------------------
+__global__ void k_validate_tris(int nt, int nv, const uint32_t *t, unsigned int *bad)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * nt)
+        return;
+    if (t[i] >= (uint32_t)nv)
+        atomicAdd(bad, 1u);
+}
+
+__global__ void k_iota(int n, int *a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        a[i] = i;
+}
+
+__global__ void k_fill_i32(size_t n, int *a, int v)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        a[i] = v;
+}
+
+__global__ void k_fill_u64(size_t n, uint64_t *a, uint64_t v)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        a[i] = v;
+}
+
+// intersecting pair j: keys ordering its pairs inside the first mesh's face (by the second triangle's order
+// key) and inside the second mesh's face (by the first triangle's order key)
+__global__ void k_pair_keys(int K, const int *__restrict__ sel, const uint64_t *__restrict__ cand, int nB,
+                            const int *__restrict__ rankA, const int *__restrict__ rankB,
+                            const double *__restrict__ seg, uint64_t *keyA, uint64_t *keyB, int *val, double *segK,
+                            uint32_t *pairAB)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= K)
+        return;
+    int idx = sel[j];
+    uint64_t key = cand[idx];
+    uint32_t a = (uint32_t)(key / (uint64_t)nB);
+    uint32_t b = (uint32_t)(key - (uint64_t)a * (uint64_t)nB);
+    uint32_t oa = rankA ? (uint32_t)rankA[a] : a;
+    uint32_t ob = rankB ? (uint32_t)rankB[b] : b;
+    keyA[j] = ((uint64_t)a << 32) | ob;
+    keyB[j] = ((uint64_t)b << 32) | oa;
+    val[j] = j;
+    for (int k = 0; k < 6; ++k)
+        segK[6 * (size_t)j + k] = seg[6 * (size_t)idx + k];
+    pairAB[2 * (size_t)j] = a;
+    pairAB[2 * (size_t)j + 1] = b;
+}
+
+__global__ void k_hi32(int n, const uint64_t *__restrict__ k, int *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = (int)(k[i] >> 32);
+}
+
+__global__ void k_face_table(int FA, int FB, const int *__restrict__ uniqA, const int *__restrict__ cntA,
+                             const int *__restrict__ uniqB, const int *__restrict__ cntB, int *faceSide,
+                             int *faceTri, int *faceCnt)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= FA + FB)
+        return;
+    if (f < FA) {
+        faceSide[f] = 0;
+        faceTri[f] = uniqA[f];
+        faceCnt[f] = cntA[f];
+    } else {
+        faceSide[f] = 1;
+        faceTri[f] = uniqB[f - FA];
+        faceCnt[f] = cntB[f - FA];
+    }
+}
+
+__global__ void k_face_status(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ status,
+                              int *firstFail)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nFaces)
+        return;
+    int st = status[f];
+    if (st == 0)
+        return;
+    if (st == 3)
+        atomicMin(firstFail + 2, f);
+    else
+        atomicMin(firstFail + faceSide[f], f);
+}
+
+__global__ void k_not_flag(int n, const int *__restrict__ flag, int *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = flag[i] ? 0 : 1;
+}
+
+__global__ void k_tri_mesh(int nTri, int uncutA, int uncutB, int retriA, int8_t *triMesh, int8_t *isUncut)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    bool first = t < uncutA || (t >= uncutA + uncutB && t < uncutA + uncutB + retriA);
+    triMesh[t] = first ? 0 : 1;
+    isUncut[t] = t < uncutA + uncutB ? 1 : 0;
+}
+
+__global__ void k_cand_pairs(int n, const uint64_t *__restrict__ cand, int nB, uint32_t *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint64_t key = cand[i];
+    uint32_t a = (uint32_t)(key / (uint64_t)nB);
+    out[2 * (size_t)i] = a;
+    out[2 * (size_t)i + 1] = (uint32_t)(key - (uint64_t)a * (uint64_t)nB);
+}
+
+} // namespace sbg
+
+using namespace sbg;
+
+// ---------------------------------------------------------------------------------------------------
+// boolean handle
+// ---------------------------------------------------------------------------------------------------
+struct sb_boolean {
+    const sb_mesh *first = nullptr, *second = nullptr;
+    sb_options opts;
+    cudaStream_t s = nullptr;
+    // working and result buffers
+    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small;
+    unsigned int candCap = 0;
+    bool combined = false;
+    sb_status status = SB_ERR_NOT_COMBINED;
+    sb_stats stats;
+    // device views kept for fetch / dumps
+    uint64_t *d_cand = nullptr;
+    int C = 0, K = 0;
+    uint32_t *d_pairAB = nullptr;
+    double *d_segK = nullptr;
+    double *d_newV = nullptr;
+    size_t nNewV = 0;
+    uint32_t *d_newT = nullptr;
+    int nTri = 0;
+    int8_t *d_label = nullptr, *d_triMesh = nullptr;
+    uint32_t *d_fetch[3] = {nullptr, nullptr, nullptr};
+    size_t nFetch[3] = {0, 0, 0};
+    cudaEvent_t ev[10];
+    bool evInit = false;
+    unsigned int *h_pinned = nullptr; // host mirror of small counters
+};
+
+namespace {
+
+template <class F> sb_status guarded(F &&f)
+{
+    try {
+        return f();
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return SB_ERR_INVALID;
+    }
+}
+
+size_t cub_need = 0;
+
+// CUB wrappers: query, grow the handle's temp buffer, run
+template <class Call> cudaError_t cub_run(sb_boolean *b, Call &&call)
+{
+    size_t need = 0;
+    cudaError_t e = call(nullptr, need);
+    if (e != cudaSuccess)
+        return e;
+    e = b->cub.ensure(need);
+    if (e != cudaSuccess)
+        return e;
+    size_t have = b->cub.bytes;
+    return call(b->cub.ptr, have);
+}
+
+sb_status read_back(sb_boolean *b, void *dst, const void *src, size_t bytes)
+{
+    SB_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(b->s));
+    return SB_OK;
+}
+
+int end_bit_for(uint64_t maxValue)
+{
+    int bits = 1;
+    while (bits < 64 && (maxValue >> bits) != 0)
+        ++bits;
+    return bits;
+}
+
+sb_status combine_impl(sb_boolean *b)
+{
+    cudaStream_t s = b->s;
+    const MeshDev &A = b->first->d;
+    const MeshDev &B = b->second->d;
+    const bool fp64 = b->opts.precision == SB_PRECISION_FP64;
+    const double factor = (double)b->opts.weld_factor;
+    sb_stats &st = b->stats;
+    std::memset(&st, 0, sizeof st);
+    b->combined = false;
+    for (int k = 0; k < 3; ++k) {
+        b->d_fetch[k] = nullptr;
+        b->nFetch[k] = 0;
+    }
+    if (!b->evInit) {
+        for (auto &e : b->ev)
+            SB_CUDA_CHECK(cudaEventCreate(&e));
+        b->evInit = true;
+    }
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[0], s));
+
+    // small device block: [0..7] stats u64, [8..] counters, firstFail, scalars
+    SB_CUDA_CHECK(b->small.ensure(4096));
+    unsigned long long *d_stats = b->small.as<unsigned long long>();
+    unsigned int *d_count = reinterpret_cast<unsigned int *>(b->small.as<char>() + 128);
+    unsigned int *d_counters = reinterpret_cast<unsigned int *>(b->small.as<char>() + 256);
+    int *d_firstFail = reinterpret_cast<int *>(b->small.as<char>() + 512);
+    int *d_scalar = reinterpret_cast<int *>(b->small.as<char>() + 640);
+    SB_CUDA_CHECK(cudaMemsetAsync(b->small.ptr, 0, 1024, s));
+
+    const int nA = A.nt, nB = B.nt;
+    // ---------------- broad phase ----------------
+    if (b->candCap == 0)
+        b->candCap = (unsigned int)std::max<size_t>(4096, 4 * ((size_t)nA + (size_t)nB));
+    unsigned int C = 0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        Carve c;
+        size_t o_raw = c.take<uint64_t>(b->candCap);
+        size_t o_srt = c.take<uint64_t>(b->candCap);
+        size_t o_hit = c.take<uint8_t>(b->candCap);
+        size_t o_seg = c.take<double>((size_t)b->candCap * 6);
+        size_t o_sel = c.take<int>(b->candCap);
+        SB_CUDA_CHECK(b->cand.ensure(c.off));
+        (void)o_hit;
+        (void)o_seg;
+        (void)o_sel;
+        SB_CUDA_CHECK(cudaMemsetAsync(d_count, 0, sizeof(unsigned int), s));
+        SB_CUDA_CHECK(cudaMemsetAsync(d_stats, 0, 8 * sizeof(unsigned long long), s));
+        launch_broad(fp64, A, B, reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw), d_count, b->candCap,
+                     d_stats, s);
+        SB_CUDA_CHECK(cudaGetLastError());
+        sb_status r = read_back(b, &C, d_count, sizeof C);
+        if (r != SB_OK)
+            return r;
+        if (C <= b->candCap)
+            break;
+        b->candCap = C + C / 4 + 1024;
+    }
+    Carve cc;
+    size_t o_raw = cc.take<uint64_t>(b->candCap);
+    size_t o_srt = cc.take<uint64_t>(b->candCap);
+    size_t o_hit = cc.take<uint8_t>(b->candCap);
+    size_t o_seg = cc.take<double>((size_t)b->candCap * 6);
+    size_t o_sel = cc.take<int>(b->candCap);
+    uint64_t *candRaw = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw);
+    uint64_t *candSorted = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_srt);
+    uint8_t *hit = reinterpret_cast<uint8_t *>(b->cand.as<char>() + o_hit);
+    double *seg = reinterpret_cast<double *>(b->cand.as<char>() + o_seg);
+    int *sel = reinterpret_cast<int *>(b->cand.as<char>() + o_sel);
+    b->C = (int)C;
+    b->d_cand = candSorted;
+    st.candidate_pairs = C;
+    const int endBit = end_bit_for((uint64_t)std::max(nA, 1) * (uint64_t)std::max(nB, 1));
+    if (C > 0)
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortKeys(tmp, bytes, candRaw, candSorted, (int)C, 0, endBit, s);
+        }));
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[1], s));
+
+    // ---------------- narrow phase ----------------
+    launch_narrow(fp64, A, B, candSorted, (int)C, hit, seg, d_stats, s);
+    SB_CUDA_CHECK(cudaGetLastError());
+    if (C > 0)
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceSelect::Flagged(tmp, bytes, thrust::counting_iterator<int>(0), hit, sel,
+                                              d_count + 1, (int)C, s);
+        }));
+    unsigned int K = 0;
+    if (C > 0) {
+        sb_status r = read_back(b, &K, d_count + 1, sizeof K);
+        if (r != SB_OK)
+            return r;
+    }
+    b->K = (int)K;
+    st.intersecting_pairs = K;
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[2], s));
+
+    // ---------------- face lists ----------------
+    Carve ci;
+    size_t o_keyA = ci.take<uint64_t>(K + 1), o_keyB = ci.take<uint64_t>(K + 1);
+    size_t o_keyAs = ci.take<uint64_t>(K + 1), o_keyBs = ci.take<uint64_t>(K + 1);
+    size_t o_val = ci.take<int>(K + 1), o_pidx = ci.take<int>(2 * (size_t)K + 2);
+    size_t o_segK = ci.take<double>(6 * (size_t)K + 6), o_ab = ci.take<uint32_t>(2 * (size_t)K + 2);
+    size_t o_hiA = ci.take<int>(K + 1), o_hiB = ci.take<int>(K + 1);
+    size_t o_uqA = ci.take<int>(K + 1), o_uqB = ci.take<int>(K + 1);
+    size_t o_ctA = ci.take<int>(K + 1), o_ctB = ci.take<int>(K + 1);
+    SB_CUDA_CHECK(b->isect.ensure(ci.off));
+    char *ib = b->isect.as<char>();
+    uint64_t *keyA = (uint64_t *)(ib + o_keyA), *keyB = (uint64_t *)(ib + o_keyB);
+    uint64_t *keyAs = (uint64_t *)(ib + o_keyAs), *keyBs = (uint64_t *)(ib + o_keyBs);
+    int *val = (int *)(ib + o_val), *pairIdx = (int *)(ib + o_pidx);
+    double *segK = (double *)(ib + o_segK);
+    uint32_t *pairAB = (uint32_t *)(ib + o_ab);
+    int *hiA = (int *)(ib + o_hiA), *hiB = (int *)(ib + o_hiB);
+    int *uqA = (int *)(ib + o_uqA), *uqB = (int *)(ib + o_uqB), *ctA = (int *)(ib + o_ctA), *ctB = (int *)(ib + o_ctB);
+    b->d_pairAB = pairAB;
+    b->d_segK = segK;
+    const bool useRank = b->opts.order == SB_ORDER_REFERENCE && A.rankValid && B.rankValid;
+    int FA = 0, FB = 0;
+    if (K > 0) {
+        k_pair_keys<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
+                                                   useRank ? B.rank : nullptr, seg, keyA, keyB, val, segK, pairAB);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
+        }));
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K, 0, 64, s);
+        }));
+        k_hi32<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
+        k_hi32<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiA, uqA, ctA, d_count + 2, (int)K, s);
+        }));
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiB, uqB, ctB, d_count + 3, (int)K, s);
+        }));
+        unsigned int runs[2];
+        sb_status r = read_back(b, runs, d_count + 2, sizeof runs);
+        if (r != SB_OK)
+            return r;
+        FA = (int)runs[0];
+        FB = (int)runs[1];
+    }
+    const int nFaces = FA + FB;
+    st.cut_faces_first = FA;
+    st.cut_faces_second = FB;
+
+    // ---------------- per-face capacities and re-triangulation ----------------
+    Carve cf;
+    size_t o_side = cf.take<int>(nFaces + 1), o_tri = cf.take<int>(nFaces + 1), o_cnt = cf.take<int>(nFaces + 1);
+    size_t o_beg = cf.take<int>(nFaces + 1), o_sb = cf.take<unsigned long long>(nFaces + 1);
+    size_t o_so = cf.take<unsigned long long>(nFaces + 1);
+    size_t o_pc = cf.take<int>(nFaces + 1), o_tc = cf.take<int>(nFaces + 1), o_ec = cf.take<int>(nFaces + 1);
+    size_t o_po = cf.take<int>(nFaces + 1), o_to = cf.take<int>(nFaces + 1), o_eo = cf.take<int>(nFaces + 1);
+    size_t o_fst = cf.take<int>(nFaces + 1), o_fnp = cf.take<int>(nFaces + 1), o_fnt = cf.take<int>(nFaces + 1);
+    size_t o_fne = cf.take<int>(nFaces + 1), o_rr = cf.take<int>(nFaces + 1);
+    SB_CUDA_CHECK(b->faces.ensure(cf.off));
+    char *fb = b->faces.as<char>();
+    int *faceSide = (int *)(fb + o_side), *faceTri = (int *)(fb + o_tri), *faceCnt = (int *)(fb + o_cnt);
+    int *faceBegin = (int *)(fb + o_beg);
+    unsigned long long *scratchBytes = (unsigned long long *)(fb + o_sb), *scratchOff = (unsigned long long *)(fb + o_so);
+    int *ptCap = (int *)(fb + o_pc), *triCapA = (int *)(fb + o_tc), *edgeCap = (int *)(fb + o_ec);
+    int *ptOff = (int *)(fb + o_po), *triOff = (int *)(fb + o_to), *edgeOff = (int *)(fb + o_eo);
+    int *faceStatus = (int *)(fb + o_fst), *faceNpts = (int *)(fb + o_fnp), *faceNtris = (int *)(fb + o_fnt);
+    int *faceNedges = (int *)(fb + o_fne), *retriRank = (int *)(fb + o_rr);
+    SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
+    long long totals[4] = {0, 0, 0, 0};
+    if (nFaces > 0) {
+        k_face_table<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
+        }));
+        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, scratchBytes, scratchOff, nFaces + 1, s);
+        }));
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, ptCap, ptOff, nFaces + 1, s);
+        }));
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, triCapA, triOff, nFaces + 1, s);
+        }));
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, edgeCap, edgeOff, nFaces + 1, s);
+        }));
+        unsigned long long sTot = 0;
+        int pTot = 0, tTot = 0, eTot = 0;
+        SB_CUDA_CHECK(cudaMemcpyAsync(&sTot, scratchOff + nFaces, sizeof sTot, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaMemcpyAsync(&pTot, ptOff + nFaces, sizeof pTot, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaMemcpyAsync(&tTot, triOff + nFaces, sizeof tTot, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaMemcpyAsync(&eTot, edgeOff + nFaces, sizeof eTot, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        totals[0] = (long long)sTot;
+        totals[1] = pTot;
+        totals[2] = tTot;
+        totals[3] = eTot;
+    }
+    Carve cu;
+    size_t o_cp = cu.take<d3>(totals[1] + 1), o_ck = cu.take<Key>(totals[1] + 1);
+    size_t o_ft = cu.take<int>(3 * totals[2] + 3), o_fe = cu.take<int>(2 * totals[3] + 2);
+    SB_CUDA_CHECK(b->cut.ensure(cu.off));
+    SB_CUDA_CHECK(b->scratch.ensure((size_t)totals[0] + 256));
+    d3 *cutPts = (d3 *)(b->cut.as<char>() + o_cp);
+    Key *cutKeys = (Key *)(b->cut.as<char>() + o_ck);
+    int *faceTris = (int *)(b->cut.as<char>() + o_ft);
+    int *faceEdges = (int *)(b->cut.as<char>() + o_fe);
+    if (nFaces > 0) {
+        FaceArgs fa;
+        fa.A = A;
+        fa.B = B;
+        fa.nFaces = nFaces;
+        fa.faceSide = faceSide;
+        fa.faceTri = faceTri;
+        fa.faceBegin = faceBegin;
+        fa.pairIdx = pairIdx;
+        fa.segs = segK;
+        fa.factor = factor;
+        fa.scratch = b->scratch.as<char>();
+        fa.scratchOff = scratchOff;
+        fa.ptOff = ptOff;
+        fa.triOff = triOff;
+        fa.edgeOff = edgeOff;
+        fa.cutPts = cutPts;
+        fa.cutKeys = cutKeys;
+        fa.faceTris = faceTris;
+        fa.faceEdges = faceEdges;
+        fa.faceStatus = faceStatus;
+        fa.faceNpts = faceNpts;
+        fa.faceNtris = faceNtris;
+        fa.faceNedges = faceNedges;
+        launch_faces(fa, s);
+        SB_CUDA_CHECK(cudaGetLastError());
+    }
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[3], s));
+
+    // ---------------- statuses ----------------
+    int firstFail[3] = {INT_MAX, INT_MAX, INT_MAX};
+    SB_CUDA_CHECK(cudaMemcpyAsync(d_firstFail, firstFail, sizeof firstFail, cudaMemcpyHostToDevice, s));
+    if (nFaces > 0)
+        k_face_status<<<blocks(nFaces, 256), 256, 0, s>>>(nFaces, faceSide, faceStatus, d_firstFail);
+
+    // ---------------- global weld ----------------
+    AsmArgs g;
+    std::memset(&g, 0, sizeof g);
+    g.A = A;
+    g.B = B;
+    g.factor = factor;
+    g.nFaces = nFaces;
+    g.faceSide = faceSide;
+    g.faceTri = faceTri;
+    g.faceNpts = faceNpts;
+    g.faceNtris = faceNtris;
+    g.faceNedges = faceNedges;
+    g.ptOff = ptOff;
+    g.triOff = triOff;
+    g.edgeOff = edgeOff;
+    g.cutPts = cutPts;
+    g.cutKeys = cutKeys;
+    g.faceTris = faceTris;
+    g.faceEdges = faceEdges;
+    g.counters = d_counters;
+    g.newBase = A.nv + B.nv;
+    const size_t nSeq = (size_t)totals[1];
+    const uint32_t weldCap = pow2_at_least(2 * nSeq + 2);
+    Carve cw;
+    size_t o_wo = cw.take<int>(weldCap), o_wm = cw.take<int>(weldCap), o_ps = cw.take<int>(nSeq + 1);
+    size_t o_if = cw.take<int>(nSeq + 1), o_fr = cw.take<int>(nSeq + 1), o_sr = cw.take<int>(weldCap);
+    SB_CUDA_CHECK(b->weld.ensure(cw.off));
+    char *wb = b->weld.as<char>();
+    g.weldOwner = (int *)(wb + o_wo);
+    g.weldMin = (int *)(wb + o_wm);
+    g.weldMask = weldCap - 1;
+    g.pointSlot = (int *)(wb + o_ps);
+    g.isFirst = (int *)(wb + o_if);
+    g.firstRank = (int *)(wb + o_fr);
+    g.slotRank = (int *)(wb + o_sr);
+    k_fill_i32<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldOwner, -1);
+    k_fill_i32<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldMin, INT_MAX);
+    SB_CUDA_CHECK(cudaMemsetAsync(g.isFirst, 0, sizeof(int) * (nSeq + 1), s));
+    launch_weld(g, s);
+    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, g.isFirst, g.firstRank, (int)nSeq + 1, s);
+    }));
+    int nNew = 0;
+    {
+        sb_status r = read_back(b, &nNew, g.firstRank + nSeq, sizeof nNew);
+        if (r != SB_OK)
+            return r;
+    }
+    g.nNew = nNew;
+    st.new_points = (uint64_t)nNew;
+    const size_t nV = (size_t)A.nv + B.nv + nNew;
+
+    // ---------------- arrangement ----------------
+    Carve ca;
+    size_t o_cA = ca.take<int>(nA + 1), o_cB = ca.take<int>(nB + 1), o_nA = ca.take<int>(nA + 1);
+    size_t o_nB = ca.take<int>(nB + 1), o_rA = ca.take<int>(nA + 1), o_rB = ca.take<int>(nB + 1);
+    SB_CUDA_CHECK(b->arr.ensure(ca.off));
+    char *ab = b->arr.as<char>();
+    g.cutA = (int *)(ab + o_cA);
+    g.cutB = (int *)(ab + o_cB);
+    int *notA = (int *)(ab + o_nA), *notB = (int *)(ab + o_nB);
+    g.uncutRankA = (int *)(ab + o_rA);
+    g.uncutRankB = (int *)(ab + o_rB);
+    SB_CUDA_CHECK(cudaMemsetAsync(g.cutA, 0, sizeof(int) * (nA + 1), s));
+    SB_CUDA_CHECK(cudaMemsetAsync(g.cutB, 0, sizeof(int) * (nB + 1), s));
+    launch_mark_cut(g, s);
+    SB_CUDA_CHECK(cudaMemsetAsync(notA, 0, sizeof(int) * (nA + 1), s));
+    SB_CUDA_CHECK(cudaMemsetAsync(notB, 0, sizeof(int) * (nB + 1), s));
+    if (nA > 0)
+        k_not_flag<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA);
+    if (nB > 0)
+        k_not_flag<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB);
+    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notA, g.uncutRankA, nA + 1, s);
+    }));
+    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notB, g.uncutRankB, nB + 1, s);
+    }));
+    if (nFaces > 0)
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceNtris, retriRank, nFaces + 1, s);
+        }));
+    int cnts[4] = {0, 0, 0, 0}; // uncutA, uncutB, retriA, retri total
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnts, g.uncutRankA + nA, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 1, g.uncutRankB + nB, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 2, retriRank + FA, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 3, retriRank + nFaces, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(firstFail, d_firstFail, sizeof firstFail, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    g.uncutA = cnts[0];
+    g.uncutB = cnts[1];
+    g.retriRank = retriRank;
+    const int nTri = cnts[0] + cnts[1] + cnts[3];
+    g.nTri = nTri;
+    b->nTri = nTri;
+
+    // results block: vertices, arrangement triangles, labels, mesh tags, fetch outputs
+    Carve cr;
+    size_t o_V = cr.take<double>(3 * nV + 3), o_T = cr.take<uint32_t>(3 * (size_t)nTri + 3);
+    size_t o_L = cr.take<int8_t>(nTri + 1), o_M = cr.take<int8_t>(nTri + 1), o_U = cr.take<int8_t>(nTri + 1);
+    size_t o_F0 = cr.take<uint32_t>(3 * (size_t)nTri + 3), o_F1 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
+    size_t o_F2 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
+    size_t o_fl = cr.take<int>(nTri + 1), o_fr2 = cr.take<int>(nTri + 1);
+    SB_CUDA_CHECK(b->res.ensure(cr.off));
+    char *rb = b->res.as<char>();
+    g.newV = (double *)(rb + o_V);
+    g.newT = (uint32_t *)(rb + o_T);
+    g.label = (int8_t *)(rb + o_L);
+    g.triMesh = (int8_t *)(rb + o_M);
+    g.isUncut = (int8_t *)(rb + o_U);
+    b->d_newV = g.newV;
+    b->nNewV = nV;
+    b->d_newT = g.newT;
+    b->d_label = g.label;
+    b->d_triMesh = g.triMesh;
+    uint32_t *fetchOut[3] = {(uint32_t *)(rb + o_F0), (uint32_t *)(rb + o_F1), (uint32_t *)(rb + o_F2)};
+    int *fFlag = (int *)(rb + o_fl), *fRank = (int *)(rb + o_fr2);
+    if (A.nv > 0)
+        SB_CUDA_CHECK(cudaMemcpyAsync(g.newV, A.v, sizeof(double) * 3 * A.nv, cudaMemcpyDeviceToDevice, s));
+    if (B.nv > 0)
+        SB_CUDA_CHECK(
+            cudaMemcpyAsync(g.newV + 3 * (size_t)A.nv, B.v, sizeof(double) * 3 * B.nv, cudaMemcpyDeviceToDevice, s));
+    launch_weld_number(g, (int)nSeq, s);
+    if (nTri > 0)
+        k_tri_mesh<<<blocks(nTri, 256), 256, 0, s>>>(nTri, cnts[0], cnts[1], cnts[2], g.triMesh, g.isUncut);
+    launch_arrangement(g, s);
+    SB_CUDA_CHECK(cudaGetLastError());
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[4], s));
+
+    // ---------------- cut loops, groups, sides ----------------
+    const uint32_t edgeCapH = pow2_at_least(2 * (size_t)totals[3] + 2);
+    const uint32_t heCap = pow2_at_least(2 * 3 * (size_t)nTri + 2);
+    Carve cg2;
+    size_t o_ek = cg2.take<uint64_t>(edgeCapH), o_ev = cg2.take<int>(edgeCapH), o_dg = cg2.take<int>(nNew + 1);
+    size_t o_hkA = cg2.take<uint64_t>(heCap), o_hvA = cg2.take<int>(heCap);
+    size_t o_hkB = cg2.take<uint64_t>(heCap), o_hvB = cg2.take<int>(heCap);
+    size_t o_par = cg2.take<int>(nTri + 1), o_sf = cg2.take<int>(nTri + 1), o_smn = cg2.take<int>(nTri + 1);
+    size_t o_rmn = cg2.take<int>(nTri + 1), o_ror = cg2.take<int>(nTri + 1), o_rep = cg2.take<int>(nTri + 1);
+    size_t o_ins = cg2.take<int>(nTri + 1);
+    SB_CUDA_CHECK(b->groups.ensure(cg2.off));
+    char *gb = b->groups.as<char>();
+    g.edgeKeys = (uint64_t *)(gb + o_ek);
+    g.edgeVals = (int *)(gb + o_ev);
+    g.edgeMask = edgeCapH - 1;
+    g.degree = (int *)(gb + o_dg);
+    g.heKeysA = (uint64_t *)(gb + o_hkA);
+    g.heValsA = (int *)(gb + o_hvA);
+    g.heKeysB = (uint64_t *)(gb + o_hkB);
+    g.heValsB = (int *)(gb + o_hvB);
+    g.heMask = heCap - 1;
+    g.parent = (int *)(gb + o_par);
+    g.seedFlag = (int *)(gb + o_sf);
+    g.seedMin = (int *)(gb + o_smn);
+    g.remMin = (int *)(gb + o_rmn);
+    g.repOfRoot = (int *)(gb + o_ror);
+    g.reps = (int *)(gb + o_rep);
+    g.insideCount = (int *)(gb + o_ins);
+    k_fill_u64<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeKeys, kEmpty64);
+    k_fill_i32<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeVals, INT_MAX);
+    SB_CUDA_CHECK(cudaMemsetAsync(g.degree, 0, sizeof(int) * (nNew + 1), s));
+    launch_loops(g, s);
+    k_fill_u64<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysA, kEmpty64);
+    k_fill_u64<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysB, kEmpty64);
+    k_fill_i32<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsA, INT_MAX);
+    k_fill_i32<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsB, INT_MAX);
+    if (nTri > 0) {
+        k_iota<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.parent);
+        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.seedMin, INT_MAX);
+        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.remMin, INT_MAX);
+        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.repOfRoot, -1);
+        SB_CUDA_CHECK(cudaMemsetAsync(g.insideCount, 0, sizeof(int) * (nTri + 1), s));
+    }
+    launch_groups(g, s);
+    SB_CUDA_CHECK(cudaGetLastError());
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[5], s));
+    unsigned int counters[kCntCount];
+    {
+        sb_status r = read_back(b, counters, d_counters, sizeof counters);
+        if (r != SB_OK)
+            return r;
+    }
+    const unsigned int nReps = counters[kCntReps];
+    launch_sides(g, nReps, fp64, s);
+    SB_CUDA_CHECK(cudaGetLastError());
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[6], s));
+
+    // ---------------- status ----------------
+    sb_status status = SB_OK;
+    if (firstFail[2] != INT_MAX)
+        status = SB_ERR_CAPACITY;
+    else if (firstFail[0] != INT_MAX || firstFail[1] != INT_MAX) {
+        int f = firstFail[0] != INT_MAX ? firstFail[0] : firstFail[1];
+        int code = 0;
+        SB_CUDA_CHECK(cudaMemcpyAsync(&code, faceStatus + f, sizeof code, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        status = code == 1 ? SB_FAIL_ATTACH : SB_FAIL_LINK;
+    } else if (counters[kCntLoopVerts + 1] != 0)
+        status = SB_FAIL_LOOP;
+
+    // ---------------- fetch ----------------
+    if (status == SB_OK && nTri > 0) {
+        for (int op = 0; op < 3; ++op) {
+            launch_fetch_flags(g, op, fFlag, s);
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, fFlag, fRank, nTri + 1, s);
+            }));
+            launch_fetch_write(g, op, fFlag, fRank, fetchOut[op], s);
+            int n = 0;
+            SB_CUDA_CHECK(cudaMemcpyAsync(&n, fRank + nTri, sizeof n, cudaMemcpyDeviceToHost, s));
+            SB_CUDA_CHECK(cudaStreamSynchronize(s));
+            b->d_fetch[op] = fetchOut[op];
+            b->nFetch[op] = (size_t)n;
+        }
+    }
+    SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));
+    unsigned long long dstats[8];
+    SB_CUDA_CHECK(cudaMemcpyAsync(dstats, d_stats, sizeof dstats, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(counters, d_counters, sizeof counters, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    SB_CUDA_CHECK(cudaGetLastError());
+    st.box_tests = dstats[0];
+    st.box_fallbacks = dstats[1];
+    st.sign_tests = dstats[2];
+    st.sign_fallbacks = dstats[3];
+    if (dstats[4] != 0 || counters[kCntSideErrors] != 0)
+        status = SB_ERR_CAPACITY;
+    st.result_vertices = nV;
+    st.result_triangles = (uint64_t)nTri;
+    st.regions_first = counters[kCntRegionsA];
+    st.regions_second = counters[kCntRegionsA + 1];
+    st.loop_vertices = counters[kCntLoopVerts];
+    st.loop_bad_degree = counters[kCntLoopVerts + 1];
+    st.duplicate_halfedges = counters[kCntDupHalfedge];
+    for (int k = 0; k < 7; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->ev[k], b->ev[k + 1]);
+        st.stage_ms[k] = ms;
+    }
+    (void)d_scalar;
+    b->status = status;
+    b->combined = true;
+    return status;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------------------------------
+// exported functions
+// ---------------------------------------------------------------------------------------------------
+extern "C" {
+
+void sb_default_options(sb_options *o)
+{
+    if (!o)
+        return;
+    o->weld_factor = 100000;
+    o->precision = SB_PRECISION_FILTERED;
+    o->order = SB_ORDER_REFERENCE;
+    o->stream = nullptr;
+}
+
+const char *sb_status_string(sb_status s)
+{
+    switch (s) {
+    case SB_OK: return "ok";
+    case SB_FAIL_ATTACH: return "attach point to triangle edge failed";
+    case SB_FAIL_LINK: return "polygon ring link failed";
+    case SB_FAIL_LOOP: return "cut edges do not form closed loops";
+    case SB_ERR_INVALID: return "invalid argument";
+    case SB_ERR_CUDA: return "CUDA error";
+    case SB_ERR_CAPACITY: return "capacity bound exceeded";
+    case SB_ERR_NOT_COMBINED: return "not combined";
+    }
+    return "unknown";
+}
+
+const char *sb_last_error(void) { return g_last_error.c_str(); }
+
+static sb_status mesh_alloc(size_t nv, size_t nt, sb_mesh **out)
+{
+    if (!out || nv > 0x7FFFFFFFu || nt > 0x2AAAAAAAu) {
+        set_last_error("mesh too large or null output");
+        return SB_ERR_INVALID;
+    }
+    auto *m = new sb_mesh;
+    m->d.nv = (int)nv;
+    m->d.nt = (int)nt;
+    cudaError_t e = m->buf.ensure(mesh_bytes((int)nv, (int)nt));
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(e, "cudaMalloc(mesh)", __FILE__, __LINE__);
+    }
+    Carve c;
+    size_t o_v = c.take<double>(nv * 3);
+    size_t o_t = c.take<uint32_t>(nt * 3);
+    m->d.v = reinterpret_cast<double *>(m->buf.as<char>() + o_v);
+    m->d.t = reinterpret_cast<uint32_t *>(m->buf.as<char>() + o_t);
+    *out = m;
+    return SB_OK;
+}
+
+static sb_status mesh_validate(sb_mesh *m, cudaStream_t s)
+{
+    if (m->d.nt == 0)
+        return SB_OK;
+    unsigned int *d_bad = nullptr;
+    SB_CUDA_CHECK(m->tmp.ensure(256));
+    d_bad = m->tmp.as<unsigned int>();
+    SB_CUDA_CHECK(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), s));
+    k_validate_tris<<<blocks(3 * (size_t)m->d.nt, 256), 256, 0, s>>>(m->d.nt, m->d.nv, m->d.t, d_bad);
+    unsigned int bad = 0;
+    SB_CUDA_CHECK(cudaMemcpyAsync(&bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (bad) {
+        set_last_error("triangle index out of range");
+        return SB_ERR_INVALID;
+    }
+    return SB_OK;
+}
+
+sb_status sb_mesh_create(const double *xyz, size_t nv, const uint32_t *tris, size_t nt, sb_mesh **out)
+{
+    return guarded([&]() -> sb_status {
+        if ((nv && !xyz) || (nt && !tris))
+            return SB_ERR_INVALID;
+        sb_status r = mesh_alloc(nv, nt, out);
+        if (r != SB_OK)
+            return r;
+        sb_mesh *m = *out;
+        if (nv)
+            SB_CUDA_CHECK(cudaMemcpy(m->d.v, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice));
+        if (nt)
+            SB_CUDA_CHECK(cudaMemcpy(m->d.t, tris, sizeof(uint32_t) * 3 * nt, cudaMemcpyHostToDevice));
+        r = mesh_validate(m, nullptr);
+        if (r != SB_OK) {
+            sb_mesh_destroy(m);
+            *out = nullptr;
+        }
+        return r;
+    });
+}
+
+sb_status sb_mesh_create_device(const double *d_xyz, size_t nv, const uint32_t *d_tris, size_t nt,
+                                const sb_options *opts, sb_mesh **out)
+{
+    return guarded([&]() -> sb_status {
+        if ((nv && !d_xyz) || (nt && !d_tris))
+            return SB_ERR_INVALID;
+        sb_status r = mesh_alloc(nv, nt, out);
+        if (r != SB_OK)
+            return r;
+        sb_mesh *m = *out;
+        cudaStream_t s = opts ? (cudaStream_t)opts->stream : nullptr;
+        m->stream = s;
+        if (nv)
+            SB_CUDA_CHECK(cudaMemcpyAsync(m->d.v, d_xyz, sizeof(double) * 3 * nv, cudaMemcpyDeviceToDevice, s));
+        if (nt)
+            SB_CUDA_CHECK(cudaMemcpyAsync(m->d.t, d_tris, sizeof(uint32_t) * 3 * nt, cudaMemcpyDeviceToDevice, s));
+        r = mesh_validate(m, s);
+        if (r != SB_OK) {
+            sb_mesh_destroy(m);
+            *out = nullptr;
+        }
+        return r;
+    });
+}
+
+sb_status sb_mesh_update_vertices_device(sb_mesh *m, const double *d_xyz, const sb_options *opts)
+{
+    if (!m || (m->d.nv && !d_xyz))
+        return SB_ERR_INVALID;
+    cudaStream_t s = opts ? (cudaStream_t)opts->stream : nullptr;
+    if (m->d.nv)
+        SB_CUDA_CHECK(cudaMemcpyAsync(m->d.v, d_xyz, sizeof(double) * 3 * m->d.nv, cudaMemcpyDeviceToDevice, s));
+    m->prepared = false;
+    return SB_OK;
+}
+
+sb_status sb_mesh_prepare(sb_mesh *m, const sb_options *opts)
+{
+    if (!m)
+        return SB_ERR_INVALID;
+    return guarded([&]() -> sb_status {
+        sb_options o;
+        sb_default_options(&o);
+        if (opts)
+            o = *opts;
+        return prepare_mesh(m, o.order, (cudaStream_t)o.stream);
+    });
+}
+
+void sb_mesh_destroy(sb_mesh *m)
+{
+    if (!m)
+        return;
+    m->buf.release();
+    m->tmp.release();
+    delete m;
+}
+
+sb_status sb_boolean_create(const sb_mesh *first, const sb_mesh *second, const sb_options *opts, sb_boolean **out)
+{
+    if (!first || !second || !out)
+        return SB_ERR_INVALID;
+    return guarded([&]() -> sb_status {
+        auto *b = new sb_boolean;
+        b->first = first;
+        b->second = second;
+        sb_default_options(&b->opts);
+        if (opts)
+            b->opts = *opts;
+        if (b->opts.weld_factor <= 0) {
+            delete b;
+            return SB_ERR_INVALID;
+        }
+        b->s = (cudaStream_t)b->opts.stream;
+        std::memset(&b->stats, 0, sizeof b->stats);
+        *out = b;
+        return SB_OK;
+    });
+}
+
+sb_status sb_combine(sb_boolean *b, sb_stats *stats)
+{
+    if (!b)
+        return SB_ERR_INVALID;
+    return guarded([&]() -> sb_status {
+        for (const sb_mesh *m : {b->first, b->second})
+            if (!m->prepared) {
+                sb_status r = prepare_mesh(const_cast<sb_mesh *>(m), b->opts.order, b->s);
+                if (r != SB_OK)
+                    return r;
+            }
+        sb_status r = combine_impl(b);
+        if (stats)
+            *stats = b->stats;
+        return r;
+    });
+}
+
+static sb_status check_fetchable(sb_boolean *b)
+{
+    if (!b)
+        return SB_ERR_INVALID;
+    if (!b->combined)
+        return SB_ERR_NOT_COMBINED;
+    return SB_OK;
+}
+
+sb_status sb_fetch(sb_boolean *b, sb_op op, uint32_t *tris, size_t cap, size_t *count)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (op < SB_UNION || op > SB_INTERSECT || !count)
+        return SB_ERR_INVALID;
+    size_t n = b->status == SB_OK ? b->nFetch[op] : 0;
+    *count = n;
+    if (!tris)
+        return SB_OK;
+    if (cap < n)
+        return SB_ERR_INVALID;
+    if (n)
+        SB_CUDA_CHECK(cudaMemcpy(tris, b->d_fetch[op], sizeof(uint32_t) * 3 * n, cudaMemcpyDeviceToHost));
+    return SB_OK;
+}
+
+sb_status sb_fetch_device(sb_boolean *b, sb_op op, const uint32_t **d_tris, size_t *count)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (op < SB_UNION || op > SB_INTERSECT || !count || !d_tris)
+        return SB_ERR_INVALID;
+    *count = b->status == SB_OK ? b->nFetch[op] : 0;
+    *d_tris = b->d_fetch[op];
+    return SB_OK;
+}
+
+sb_status sb_result_vertices(sb_boolean *b, double *xyz, size_t cap, size_t *count)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (!count)
+        return SB_ERR_INVALID;
+    *count = b->nNewV;
+    if (!xyz)
+        return SB_OK;
+    if (cap < b->nNewV)
+        return SB_ERR_INVALID;
+    if (b->nNewV)
+        SB_CUDA_CHECK(cudaMemcpy(xyz, b->d_newV, sizeof(double) * 3 * b->nNewV, cudaMemcpyDeviceToHost));
+    return SB_OK;
+}
+
+sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t *count)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (!count || !d_xyz)
+        return SB_ERR_INVALID;
+    *count = b->nNewV;
+    *d_xyz = b->d_newV;
+    return SB_OK;
+}
+
+sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (!name || !bytes)
+        return SB_ERR_INVALID;
+    std::string n(name);
+    const void *src = nullptr;
+    size_t sz = 0;
+    DevBuf tmp;
+    if (n == "candidates") {
+        sz = sizeof(uint32_t) * 2 * (size_t)b->C;
+        if (out && sz) {
+            SB_CUDA_CHECK(tmp.ensure(sz));
+            k_cand_pairs<<<blocks(b->C, 256), 256, 0, b->s>>>(b->C, b->d_cand, b->second->d.nt, tmp.as<uint32_t>());
+            SB_CUDA_CHECK(cudaStreamSynchronize(b->s));
+            src = tmp.ptr;
+        }
+    } else if (n == "intersection_pairs") {
+        sz = sizeof(uint32_t) * 2 * (size_t)b->K;
+        src = b->d_pairAB;
+    } else if (n == "intersection_segments") {
+        sz = sizeof(double) * 6 * (size_t)b->K;
+        src = b->d_segK;
+    } else if (n == "arrangement") {
+        sz = sizeof(uint32_t) * 3 * (size_t)b->nTri;
+        src = b->d_newT;
+    } else if (n == "labels") {
+        sz = (size_t)b->nTri;
+        src = b->d_label;
+    } else if (n == "tri_mesh") {
+        sz = (size_t)b->nTri;
+        src = b->d_triMesh;
+    } else {
+        return SB_ERR_INVALID;
+    }
+    *bytes = sz;
+    if (!out || !sz) {
+        tmp.release();
+        return SB_OK;
+    }
+    if (cap_bytes < sz) {
+        tmp.release();
+        return SB_ERR_INVALID;
+    }
+    cudaError_t e = cudaMemcpy(out, src, sz, cudaMemcpyDeviceToHost);
+    tmp.release();
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(dump)", __FILE__, __LINE__);
+    return SB_OK;
+}
+
+void sb_boolean_destroy(sb_boolean *b)
+{
+    if (!b)
+        return;
+    for (DevBuf *d : {&b->cand, &b->isect, &b->faces, &b->scratch, &b->cut, &b->weld, &b->arr, &b->groups, &b->res,
+                      &b->cub, &b->small})
+        d->release();
+    if (b->evInit)
+        for (auto &e : b->ev)
+            cudaEventDestroy(e);
+    delete b;
+}
+
+} // extern "C"

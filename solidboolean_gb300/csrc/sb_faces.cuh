@@ -1,0 +1,34 @@
+// Per-face re-triangulation launch interface.
+#pragma once
+#include "sb_common.cuh"
+#include "sb_internal.h"
+
+namespace sbg {
+
+struct FaceJob {
+    int side, tri, pairBegin, pairEnd;
+};
+
+struct FaceArgs {
+    MeshDev A, B;
+    int nFaces;
+    const int *faceSide, *faceTri, *faceBegin; // faceBegin has nFaces + 1 entries
+    const int *pairIdx;                        // per face, its pairs (indices into segs) in processing order
+    const double *segs;                        // [K*6]
+    double factor;
+    char *scratch;
+    const unsigned long long *scratchOff;
+    const int *ptOff, *triOff, *edgeOff;       // exclusive prefix sums of the capacities (nFaces + 1)
+    d3 *cutPts;
+    Key *cutKeys;
+    int *faceTris;                             // local ids, 3 per triangle
+    int *faceEdges;                            // local ids, 2 per edge
+    int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
+};
+
+size_t face_scratch_bytes_host(int np);
+void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
+                       int *edgeCap, cudaStream_t s);
+void launch_faces(const FaceArgs &a, cudaStream_t s);
+
+} // namespace sbg

@@ -1,0 +1,77 @@
+// Internal host-side structures shared by the .cu translation units (not part of the C ABI).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/solidboolean_gb300.h"
+
+namespace sbg {
+
+sb_status cuda_fail(cudaError_t e, const char *expr, const char *file, int line);
+void set_last_error(const std::string &msg);
+
+// Device memory block owned by a mesh or a boolean. Grows by reallocation only (never shrinks).
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need);
+    void release();
+    template <class T> T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+// Bump allocator over one DevBuf; offsets are 256-byte aligned.
+struct Carve {
+    size_t off = 0;
+    template <class T> size_t take(size_t count)
+    {
+        size_t o = off;
+        off += (count * sizeof(T) + 255) & ~size_t(255);
+        return o;
+    }
+};
+
+// LBVH over the triangles of one mesh. Internal nodes 0..n-2 (root 0); a child index c >= 0 is an internal
+// node and c < 0 is the leaf ~c (position in Morton order). FP32 node boxes are rounded outward (they only
+// prune); FP64 node boxes are exact unions (plain FP64 form).
+struct MeshDev {
+    int nv = 0, nt = 0;
+    double *v = nullptr;      // [nv*3] FP64 xyz
+    uint32_t *t = nullptr;    // [nt*3]
+    float4 *vf = nullptr;     // [nv] FP32 copy (round to nearest) for the filtered predicates
+    double *box64 = nullptr;  // [nt*6] lo xyz, hi xyz
+    float *box32 = nullptr;   // [nt*6] round-to-nearest copy of box64
+    uint32_t *morton = nullptr;
+    int *leafTri = nullptr;   // [nt] triangle at each Morton-ordered leaf
+    int2 *child = nullptr;    // [nt-1] (left, right)
+    int *parent = nullptr;    // [2*nt-1]: internal nodes then leaves (offset nt-1)
+    float *nbox32 = nullptr;  // [(nt-1)*6]
+    double *nbox64 = nullptr; // [(nt-1)*6]
+    int *flags = nullptr;     // [nt-1] refit arrival counters
+    int *rank = nullptr;      // [nt] position of each triangle in the reference tree's leaf order
+    bool rankValid = false;
+    int root = 0;             // 0, or ~0 when nt == 1
+};
+
+struct sb_mesh_impl;
+} // namespace sbg
+
+struct sb_mesh {
+    sbg::MeshDev d;
+    sbg::DevBuf buf;
+    sbg::DevBuf tmp;
+    bool prepared = false;
+    bool ownsInput = true;
+    cudaStream_t stream = nullptr;
+    std::vector<double> hostV;    // only for host-created meshes (kept for re-preparation)
+    std::vector<uint32_t> hostT;
+};
+
+namespace sbg {
+// sb_prepare.cu
+sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s);
+// sb_refrank.cu: position of each triangle in the reference tree's leaf order
+sb_status build_reference_rank(sb_mesh *m, cudaStream_t s);
+} // namespace sbg

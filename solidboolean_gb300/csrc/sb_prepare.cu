@@ -1,0 +1,315 @@
+// Mesh preparation on the GPU (the counterpart of SolidMesh::prepare, src/solidmesh.cpp:42-76).
+//
+// The reference builds unit normals, per-triangle AABBs and a top-down AABB tree. Here:
+//   * per-triangle AABBs (exact FP64 min/max, plus a round-to-nearest FP32 copy for the filtered tests);
+//   * an LBVH: 30-bit Morton codes of the FP32 box centres, a radix sort, Karras' hierarchy construction
+//     (one thread per internal node) and a bottom-up refit in which the second child to arrive at a node
+//     (atomic counter) writes the union box;
+//   * unit normals are not stored: the kernels that need one recompute it with the reference's formula.
+// The reference tree's leaf order, needed only to reproduce its per-face pair order, is built by
+// sb_refrank.cu.
+#include <cub/cub.cuh>
+
+#include "sb_common.cuh"
+#include "sb_internal.h"
+
+namespace sbg {
+
+__global__ void k_vertices_f32(int nv, const double *__restrict__ v, float4 *__restrict__ vf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv)
+        return;
+    vf[i] = make_float4(__double2float_rn(v[3 * i]), __double2float_rn(v[3 * i + 1]),
+                        __double2float_rn(v[3 * i + 2]), 0.0f);
+}
+
+// Per-triangle box, updated vertex by vertex like AxisAlignedBoudingBox::update
+// (src/axisalignedboundingbox.h:31-41), and the FP32 box centre used for the Morton code.
+__global__ void k_tri_boxes(int nt, const double *__restrict__ v, const uint32_t *__restrict__ t,
+                            double *__restrict__ box64, float *__restrict__ box32, float *__restrict__ cen,
+                            unsigned int *__restrict__ bounds)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float c[3] = {0.f, 0.f, 0.f};
+    bool valid = i < nt;
+    if (valid) {
+        double lo[3] = {kDblMax, kDblMax, kDblMax};
+        double hi[3] = {-kDblMax, -kDblMax, -kDblMax};
+        for (int k = 0; k < 3; ++k) {
+            const double *p = v + 3 * (size_t)t[3 * i + k];
+            for (int a = 0; a < 3; ++a) {
+                double x = p[a];
+                if (x > hi[a])
+                    hi[a] = x;
+                if (x < lo[a])
+                    lo[a] = x;
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            box64[6 * (size_t)i + a] = lo[a];
+            box64[6 * (size_t)i + 3 + a] = hi[a];
+            float l = __double2float_rn(lo[a]), h = __double2float_rn(hi[a]);
+            box32[6 * (size_t)i + a] = l;
+            box32[6 * (size_t)i + 3 + a] = h;
+            c[a] = 0.5f * l + 0.5f * h;
+            cen[3 * (size_t)i + a] = c[a];
+        }
+    }
+    // block-wide min/max of the centres, then one atomic per block and axis (ordered-int encoding)
+    __shared__ unsigned int smin[3][32], smax[3][32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int a = 0; a < 3; ++a) {
+        unsigned int u = __float_as_uint(c[a]);
+        unsigned int o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        unsigned int mn = valid ? o : 0xFFFFFFFFu, mx = valid ? o : 0u;
+        for (int s = 16; s > 0; s >>= 1) {
+            mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, s));
+            mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, s));
+        }
+        if (lane == 0) {
+            smin[a][warp] = mn;
+            smax[a][warp] = mx;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int a = threadIdx.x;
+        unsigned int mn = 0xFFFFFFFFu, mx = 0u;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            mn = min(mn, smin[a][w]);
+            mx = max(mx, smax[a][w]);
+        }
+        atomicMin(bounds + a, mn);
+        atomicMax(bounds + 3 + a, mx);
+    }
+}
+
+__device__ __forceinline__ float ord_to_float(unsigned int o)
+{
+    unsigned int u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+    return __uint_as_float(u);
+}
+
+__device__ __forceinline__ uint32_t expand10(uint32_t x)
+{
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void k_morton(int nt, const float *__restrict__ cen, const unsigned int *__restrict__ bounds,
+                         uint32_t *__restrict__ code, int *__restrict__ idx)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt)
+        return;
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        float lo = ord_to_float(bounds[a]), hi = ord_to_float(bounds[3 + a]);
+        float ext = hi - lo;
+        float u = ext > 0.f ? (cen[3 * (size_t)i + a] - lo) / ext : 0.f;
+        int k = (int)(u * 1024.0f);
+        q[a] = (uint32_t)min(max(k, 0), 1023);
+    }
+    code[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+    idx[i] = i;
+}
+
+// common-prefix length of the (code, index) keys of leaves i and j; -1 outside [0, n)
+__device__ __forceinline__ int lbvh_delta(const uint32_t *code, int n, int i, int j)
+{
+    if (j < 0 || j >= n)
+        return -1;
+    uint32_t a = code[i], b = code[j];
+    if (a == b)
+        return 32 + __clz((unsigned)(i ^ j));
+    return __clz(a ^ b);
+}
+
+// Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d trees".
+__global__ void k_karras(int n, const uint32_t *__restrict__ code, int2 *__restrict__ child, int *__restrict__ parent)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1)
+        return;
+    int d = (lbvh_delta(code, n, i, i + 1) - lbvh_delta(code, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = lbvh_delta(code, n, i, i - d);
+    int lmax = 2;
+    while (lbvh_delta(code, n, i, i + lmax * d) > dmin)
+        lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (lbvh_delta(code, n, i, i + (l + t) * d) > dmin)
+            l += t;
+    int j = i + l * d;
+    int dnode = lbvh_delta(code, n, i, j);
+    int s = 0;
+    int div = 2;
+    int t = (l + div - 1) / div;
+    while (true) {
+        if (lbvh_delta(code, n, i, i + (s + t) * d) > dnode)
+            s += t;
+        if (t == 1)
+            break;
+        div <<= 1;
+        t = (l + div - 1) / div;
+    }
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int left = (lo == gamma) ? ~gamma : gamma;
+    int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    child[i] = make_int2(left, right);
+    parent[left >= 0 ? left : (n - 1) + ~left] = i;
+    parent[right >= 0 ? right : (n - 1) + ~right] = i;
+}
+
+__device__ __forceinline__ void load_child_boxes(int c, const int *leafTri, const double *box64, const double *nbox64,
+                                                 const float *nbox32, double *b64, float *b32)
+{
+    if (c < 0) {
+        int tri = leafTri[~c];
+        for (int k = 0; k < 6; ++k)
+            b64[k] = __ldcg(box64 + 6 * (size_t)tri + k);
+        for (int k = 0; k < 3; ++k) {
+            b32[k] = __double2float_rd(b64[k]);
+            b32[3 + k] = __double2float_ru(b64[3 + k]);
+        }
+    } else {
+        for (int k = 0; k < 6; ++k) {
+            b64[k] = __ldcg(nbox64 + 6 * (size_t)c + k);
+            b32[k] = __ldcg(nbox32 + 6 * (size_t)c + k);
+        }
+    }
+}
+
+// Bottom-up refit: the second thread to reach a node writes the union of its children's boxes.
+__global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__restrict__ box64,
+                        const int2 *__restrict__ child, const int *__restrict__ parent, int *flags, double *nbox64,
+                        float *nbox32)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int node = parent[(n - 1) + i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0)
+            return;
+        __threadfence();
+        int2 ch = child[node];
+        double a64[6], b64[6];
+        float a32[6], b32[6];
+        load_child_boxes(ch.x, leafTri, box64, nbox64, nbox32, a64, a32);
+        load_child_boxes(ch.y, leafTri, box64, nbox64, nbox32, b64, b32);
+        for (int k = 0; k < 3; ++k) {
+            nbox64[6 * (size_t)node + k] = fmin(a64[k], b64[k]);
+            nbox64[6 * (size_t)node + 3 + k] = fmax(a64[3 + k], b64[3 + k]);
+            nbox32[6 * (size_t)node + k] = fminf(a32[k], b32[k]);
+            nbox32[6 * (size_t)node + 3 + k] = fmaxf(a32[3 + k], b32[3 + k]);
+        }
+        node = parent[node];
+    }
+}
+
+static inline int blocks_for(size_t n, int bs) { return (int)((n + bs - 1) / bs); }
+
+sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
+{
+    MeshDev &d = m->d;
+    const int nt = d.nt;
+    if (nt <= 0) {
+        m->prepared = true;
+        return SB_OK;
+    }
+    // layout of the prepared arrays after the input arrays (v, t) already in m->buf
+    Carve c;
+    size_t o_v = c.take<double>((size_t)d.nv * 3);
+    size_t o_t = c.take<uint32_t>((size_t)nt * 3);
+    size_t o_vf = c.take<float4>((size_t)d.nv);
+    size_t o_b64 = c.take<double>((size_t)nt * 6);
+    size_t o_b32 = c.take<float>((size_t)nt * 6);
+    size_t o_mc = c.take<uint32_t>((size_t)nt);
+    size_t o_lt = c.take<int>((size_t)nt);
+    size_t o_ch = c.take<int2>((size_t)(nt > 1 ? nt - 1 : 1));
+    size_t o_pa = c.take<int>((size_t)(2 * nt));
+    size_t o_n32 = c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    size_t o_n64 = c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    size_t o_fl = c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
+    size_t o_rk = c.take<int>((size_t)nt);
+    (void)o_v;
+    (void)o_t;
+    if (m->buf.bytes < c.off) {
+        // inputs live at the front of buf; grow while keeping them
+        DevBuf nb;
+        SB_CUDA_CHECK(nb.ensure(c.off));
+        SB_CUDA_CHECK(cudaMemcpyAsync(nb.ptr, m->buf.ptr, o_vf, cudaMemcpyDeviceToDevice, s));
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        m->buf.release();
+        m->buf = nb;
+        d.v = m->buf.as<double>();
+        d.t = reinterpret_cast<uint32_t *>(m->buf.as<char>() + o_t);
+    }
+    char *base = m->buf.as<char>();
+    d.vf = reinterpret_cast<float4 *>(base + o_vf);
+    d.box64 = reinterpret_cast<double *>(base + o_b64);
+    d.box32 = reinterpret_cast<float *>(base + o_b32);
+    d.morton = reinterpret_cast<uint32_t *>(base + o_mc);
+    d.leafTri = reinterpret_cast<int *>(base + o_lt);
+    d.child = reinterpret_cast<int2 *>(base + o_ch);
+    d.parent = reinterpret_cast<int *>(base + o_pa);
+    d.nbox32 = reinterpret_cast<float *>(base + o_n32);
+    d.nbox64 = reinterpret_cast<double *>(base + o_n64);
+    d.flags = reinterpret_cast<int *>(base + o_fl);
+    d.rank = reinterpret_cast<int *>(base + o_rk);
+
+    // temporaries: centres, bounds, unsorted keys/indices, CUB scratch
+    size_t sortBytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, (uint32_t *)nullptr, (uint32_t *)nullptr, (int *)nullptr,
+                                    (int *)nullptr, nt, 0, 30, s);
+    Carve tc;
+    size_t t_cen = tc.take<float>((size_t)nt * 3);
+    size_t t_bnd = tc.take<unsigned int>(8);
+    size_t t_key = tc.take<uint32_t>((size_t)nt);
+    size_t t_idx = tc.take<int>((size_t)nt);
+    size_t t_cub = tc.take<char>(sortBytes);
+    SB_CUDA_CHECK(m->tmp.ensure(tc.off));
+    char *tb = m->tmp.as<char>();
+    float *cen = reinterpret_cast<float *>(tb + t_cen);
+    unsigned int *bounds = reinterpret_cast<unsigned int *>(tb + t_bnd);
+    uint32_t *keyIn = reinterpret_cast<uint32_t *>(tb + t_key);
+    int *idxIn = reinterpret_cast<int *>(tb + t_idx);
+
+    const int BS = 256;
+    k_vertices_f32<<<blocks_for(d.nv, BS), BS, 0, s>>>(d.nv, d.v, d.vf);
+    unsigned int initB[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
+    SB_CUDA_CHECK(cudaMemcpyAsync(bounds, initB, sizeof initB, cudaMemcpyHostToDevice, s));
+    k_tri_boxes<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.v, d.t, d.box64, d.box32, cen, bounds);
+    k_morton<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
+    SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tb + t_cub, sortBytes, keyIn, d.morton, idxIn, d.leafTri, nt, 0,
+                                                  30, s));
+    if (nt > 1) {
+        SB_CUDA_CHECK(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * 2 * (size_t)nt, s));
+        SB_CUDA_CHECK(cudaMemsetAsync(d.flags, 0, sizeof(int) * (size_t)(nt - 1), s));
+        k_karras<<<blocks_for(nt - 1, BS), BS, 0, s>>>(nt, d.morton, d.child, d.parent);
+        k_refit<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.leafTri, d.box64, d.child, d.parent, d.flags, d.nbox64,
+                                                  d.nbox32);
+        d.root = 0;
+    } else {
+        d.root = ~0;
+    }
+    SB_CUDA_CHECK(cudaGetLastError());
+    d.rankValid = false;
+    if (order_mode == SB_ORDER_REFERENCE) {
+        sb_status st = build_reference_rank(m, s);
+        if (st != SB_OK)
+            return st;
+    }
+    m->prepared = true;
+    return SB_OK;
+}
+
+} // namespace sbg
