@@ -86,6 +86,13 @@ typedef struct sb_stats {
 void sb_default_options(sb_options *opts);
 const char *sb_status_string(sb_status s);
 const char *sb_last_error(void);
+/* Number of this library's own kernel launches since load (sort/scan primitives excluded). */
+uint64_t sb_kernel_launches(void);
+/* Diagnostic device timing of the main kernels: enable (clears earlier records), then read the summed
+ * event time and launch count of one kernel by name (synchronises), or the comma-separated names seen. */
+void sb_kernel_timing(int enable);
+int sb_kernel_timing_read(const char *name, double *total_ms, uint64_t *launches);
+int sb_kernel_timing_names(char *buf, size_t cap);
 
 /* Mesh: vertices are FP64 xyz triplets, triangles are uint32 index triplets. The host variant copies
  * the arrays; the device variant copies from device pointers on opts->stream. */
@@ -106,10 +113,11 @@ sb_status sb_result_vertices(sb_boolean *b, double *xyz, size_t cap, size_t *cou
 /* Device results: pointers stay valid until the next combine or destroy; counts are host values. */
 sb_status sb_fetch_device(sb_boolean *b, sb_op op, const uint32_t **d_tris, size_t *count);
 sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t *count);
-/* Stage dumps for parity checks (host copies). Names: "candidates" (uint32 pairs), "intersections"
- * (uint32 pair + 6 doubles as raw bytes), "arrangement" (uint32 triangles), "labels" (int8 per arrangement
- * triangle: 0 outside, 1 inside, -1 ungrouped), "first_range" (uint32 start/count of the first mesh's
- * triangles in the arrangement). *bytes receives the size; out may be NULL. */
+/* Stage dumps for parity checks (host copies). Names: "candidates" (uint32 pairs, sorted),
+ * "intersection_pairs" (uint32 pairs), "intersection_segments" (6 doubles per intersecting pair),
+ * "arrangement" (uint32 triangles), "labels" (int8 per arrangement triangle: 0 outside, 1 inside, -1 in no
+ * group), "tri_mesh" (int8 per arrangement triangle: 0 first mesh, 1 second). *bytes receives the size;
+ * out may be NULL. */
 sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
 void sb_boolean_destroy(sb_boolean *b);
 

@@ -27,7 +27,8 @@ SB_UNION, SB_DIFF, SB_INTERSECT = 0, 1, 2
 PRECISION = {"filtered": 0, "fp64": 1}
 ORDER = {"reference": 0, "index": 1}
 
-EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_mesh_create", "sb_mesh_create_device",
+EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_kernel_launches", "sb_mesh_create",
+           "sb_mesh_create_device",
            "sb_mesh_update_vertices_device", "sb_mesh_prepare", "sb_mesh_destroy", "sb_boolean_create",
            "sb_combine", "sb_fetch", "sb_result_vertices", "sb_fetch_device", "sb_result_vertices_device",
            "sb_debug_dump", "sb_boolean_destroy"]
@@ -71,6 +72,7 @@ def lib() -> ctypes.CDLL:
     L.sb_status_string.restype = ctypes.c_char_p
     L.sb_status_string.argtypes = [st]
     L.sb_last_error.restype = ctypes.c_char_p
+    L.sb_kernel_launches.restype = ctypes.c_uint64
     L.sb_mesh_create.restype = st
     L.sb_mesh_create.argtypes = [vp, sz, vp, sz, ctypes.POINTER(vp)]
     L.sb_mesh_create_device.restype = st

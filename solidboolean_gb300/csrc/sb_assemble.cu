@@ -16,6 +16,7 @@
 
 #include "sb_assemble.cuh"
 #include "sb_common.cuh"
+#include "sb_ktime.h"
 
 namespace sbg {
 
@@ -522,66 +523,113 @@ void launch_weld(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nFaces <= 0)
         return;
-    k_weld_insert<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.cutKeys, g.weldOwner, g.weldMin,
+    {
+        KTime kt("k_weld_insert", s);
+        SB_COUNT(k_weld_insert)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.cutKeys, g.weldOwner, g.weldMin,
                                           g.weldMask, g.pointSlot);
-    k_weld_first<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.pointSlot, g.weldMin, g.isFirst);
+    }
+    {
+        KTime kt("k_weld_first", s);
+        SB_COUNT(k_weld_first)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.pointSlot, g.weldMin, g.isFirst);
+    }
 }
 
 void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s)
 {
     if (nSeq <= 0)
         return;
-    k_weld_number<<<nb(nSeq, 256), 256, 0, s>>>(nSeq, g.isFirst, g.firstRank, g.pointSlot, g.slotRank, g.cutPts,
+    {
+        KTime kt("k_weld_number", s);
+        SB_COUNT(k_weld_number)<<<nb(nSeq, 256), 256, 0, s>>>(nSeq, g.isFirst, g.firstRank, g.pointSlot, g.slotRank, g.cutPts,
                                                 g.newV, g.newBase);
+    }
 }
 
 void launch_mark_cut(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nFaces > 0)
-        k_mark_cut<<<nb(g.nFaces, 256), 256, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.cutA, g.cutB);
+        {
+            KTime kt("k_mark_cut", s);
+            SB_COUNT(k_mark_cut)<<<nb(g.nFaces, 256), 256, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.cutA, g.cutB);
+        }
 }
 
 void launch_arrangement(const AsmArgs &g, cudaStream_t s)
 {
     if (g.A.nt > 0)
-        k_uncut<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT);
+        {
+            KTime kt("k_uncut", s);
+            SB_COUNT(k_uncut)<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT);
+        }
     if (g.B.nt > 0)
-        k_uncut<<<nb(g.B.nt, 256), 256, 0, s>>>(g.B.nt, g.B.t, g.cutB, g.uncutRankB, (uint32_t)g.A.nv,
+        {
+            KTime kt("k_uncut", s);
+            SB_COUNT(k_uncut)<<<nb(g.B.nt, 256), 256, 0, s>>>(g.B.nt, g.B.t, g.cutB, g.uncutRankB, (uint32_t)g.A.nv,
                                                 (uint32_t)g.uncutA, g.newT);
+        }
     if (g.nFaces > 0)
-        k_retri<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.faceNtris, g.triOff, g.retriRank,
+        {
+            KTime kt("k_retri", s);
+            SB_COUNT(k_retri)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.faceNtris, g.triOff, g.retriRank,
                                         g.faceTris, g.ptOff, g.pointSlot, g.slotRank, g.A, g.B,
                                         (uint32_t)g.newBase, (uint32_t)(g.uncutA + g.uncutB), g.newT);
+        }
 }
 
 void launch_loops(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nFaces > 0)
-        k_cut_edges<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceNedges, g.edgeOff, g.faceEdges, g.ptOff,
+        {
+            KTime kt("k_cut_edges", s);
+            SB_COUNT(k_cut_edges)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceNedges, g.edgeOff, g.faceEdges, g.ptOff,
                                             g.pointSlot, g.slotRank, g.edgeKeys, g.edgeVals, g.edgeMask, 0);
-    k_loop_degree<<<nb((size_t)g.edgeMask + 1, 256), 256, 0, s>>>(g.edgeMask + 1, g.edgeKeys, g.degree);
+        }
+    {
+        KTime kt("k_loop_degree", s);
+        SB_COUNT(k_loop_degree)<<<nb((size_t)g.edgeMask + 1, 256), 256, 0, s>>>(g.edgeMask + 1, g.edgeKeys, g.degree);
+    }
     if (g.nNew > 0)
-        k_loop_check<<<nb(g.nNew, 256), 256, 0, s>>>(g.nNew, g.degree, g.counters + kCntLoopVerts);
+        {
+            KTime kt("k_loop_check", s);
+            SB_COUNT(k_loop_check)<<<nb(g.nNew, 256), 256, 0, s>>>(g.nNew, g.degree, g.counters + kCntLoopVerts);
+        }
 }
 
 void launch_groups(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nTri <= 0)
         return;
-    k_halfedges<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
+    {
+        KTime kt("k_halfedges", s);
+        SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
                                                 g.heValsB, g.heMask);
-    k_union<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
+    }
+    {
+        KTime kt("k_union", s);
+        SB_COUNT(k_union)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
                                             g.heMask, g.edgeKeys, g.edgeVals, g.edgeMask, (uint32_t)g.newBase,
                                             g.parent, g.seedFlag, g.counters + kCntDupHalfedge);
-    k_uf_flatten<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent);
-    k_region_rep<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedFlag, g.isUncut, g.seedMin, g.remMin);
-    k_region_list<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot, g.reps,
+    }
+    {
+        KTime kt("k_uf_flatten", s);
+        SB_COUNT(k_uf_flatten)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent);
+    }
+    {
+        KTime kt("k_region_rep", s);
+        SB_COUNT(k_region_rep)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedFlag, g.isUncut, g.seedMin, g.remMin);
+    }
+    {
+        KTime kt("k_region_list", s);
+        SB_COUNT(k_region_list)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot, g.reps,
                                                   g.counters + kCntReps, g.triMesh, g.counters + kCntRegionsA);
+    }
 }
 
 void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s)
 {
     if (nReps > 0) {
+        KTime kt("k_sides", s);
+        count_launch();
         if (fp64)
             k_sides<true><<<nb(3 * (size_t)nReps, 64), 64, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
                                                                    g.triMesh, g.A, g.B, g.factor, g.insideCount,
@@ -592,19 +640,28 @@ void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t 
                                                                     g.counters + kCntSideErrors);
     }
     if (g.nTri > 0)
-        k_labels<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.repOfRoot, g.insideCount, g.label);
+        {
+            KTime kt("k_labels", s);
+            SB_COUNT(k_labels)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.repOfRoot, g.insideCount, g.label);
+        }
 }
 
 void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s)
 {
     if (g.nTri > 0)
-        k_fetch_flags<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.label, g.triMesh, op, flag);
+        {
+            KTime kt("k_fetch_flags", s);
+            SB_COUNT(k_fetch_flags)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.label, g.triMesh, op, flag);
+        }
 }
 
 void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s)
 {
     if (g.nTri > 0)
-        k_fetch_write<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, flag, rank, g.newT, g.triMesh, op, out);
+        {
+            KTime kt("k_fetch_write", s);
+            SB_COUNT(k_fetch_write)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, flag, rank, g.newT, g.triMesh, op, out);
+        }
 }
 
 } // namespace sbg

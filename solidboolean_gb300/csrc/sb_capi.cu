@@ -5,6 +5,7 @@
 // arrangement, cut-loop check, union-find regions, side rays, fetch compaction. The host only reads the
 // handful of counts that size the next stage (candidates, intersecting pairs, faces, per-face totals).
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -23,8 +24,44 @@
 namespace sbg {
 
 static thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ---- per-kernel timing registry ----------------------------------------------------------------------
+struct KRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+static std::mutex g_kt_mutex;
+static std::vector<KRec> g_kt_recs;
+static size_t g_kt_used = 0;
+static std::atomic<bool> g_kt_on{false};
+
+bool ktime_enabled() { return g_kt_on.load(std::memory_order_relaxed); }
+
+int ktime_begin(const char *name, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    if (g_kt_used == g_kt_recs.size()) {
+        KRec r;
+        if (cudaEventCreate(&r.a) != cudaSuccess || cudaEventCreate(&r.b) != cudaSuccess)
+            return -1;
+        g_kt_recs.push_back(r);
+    }
+    KRec &r = g_kt_recs[g_kt_used];
+    r.name = name;
+    cudaEventRecord(r.a, s);
+    return (int)g_kt_used++;
+}
+
+void ktime_end(int id, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    if (id >= 0 && (size_t)id < g_kt_used)
+        cudaEventRecord(g_kt_recs[id].b, s);
+}
 
 sb_status cuda_fail(cudaError_t e, const char *expr, const char *file, int line)
 {
@@ -407,7 +444,7 @@ sb_status combine_impl(sb_boolean *b)
     const bool useRank = b->opts.order == SB_ORDER_REFERENCE && A.rankValid && B.rankValid;
     int FA = 0, FB = 0;
     if (K > 0) {
-        k_pair_keys<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
+        SB_COUNT(k_pair_keys)<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
                                                    useRank ? B.rank : nullptr, seg, keyA, keyB, val, segK, pairAB);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
@@ -415,8 +452,8 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K, 0, 64, s);
         }));
-        k_hi32<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
-        k_hi32<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
+        SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
+        SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiA, uqA, ctA, d_count + 2, (int)K, s);
         }));
@@ -455,7 +492,7 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
     long long totals[4] = {0, 0, 0, 0};
     if (nFaces > 0) {
-        k_face_table<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
+        SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
         }));
@@ -526,7 +563,7 @@ sb_status combine_impl(sb_boolean *b)
     int firstFail[3] = {INT_MAX, INT_MAX, INT_MAX};
     SB_CUDA_CHECK(cudaMemcpyAsync(d_firstFail, firstFail, sizeof firstFail, cudaMemcpyHostToDevice, s));
     if (nFaces > 0)
-        k_face_status<<<blocks(nFaces, 256), 256, 0, s>>>(nFaces, faceSide, faceStatus, d_firstFail);
+        SB_COUNT(k_face_status)<<<blocks(nFaces, 256), 256, 0, s>>>(nFaces, faceSide, faceStatus, d_firstFail);
 
     // ---------------- global weld ----------------
     AsmArgs g;
@@ -563,8 +600,8 @@ sb_status combine_impl(sb_boolean *b)
     g.isFirst = (int *)(wb + o_if);
     g.firstRank = (int *)(wb + o_fr);
     g.slotRank = (int *)(wb + o_sr);
-    k_fill_i32<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldOwner, -1);
-    k_fill_i32<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldMin, INT_MAX);
+    SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldOwner, -1);
+    SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldMin, INT_MAX);
     SB_CUDA_CHECK(cudaMemsetAsync(g.isFirst, 0, sizeof(int) * (nSeq + 1), s));
     launch_weld(g, s);
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
@@ -597,9 +634,9 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemsetAsync(notA, 0, sizeof(int) * (nA + 1), s));
     SB_CUDA_CHECK(cudaMemsetAsync(notB, 0, sizeof(int) * (nB + 1), s));
     if (nA > 0)
-        k_not_flag<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA);
+        SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA);
     if (nB > 0)
-        k_not_flag<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB);
+        SB_COUNT(k_not_flag)<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB);
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, notA, g.uncutRankA, nA + 1, s);
     }));
@@ -652,7 +689,7 @@ sb_status combine_impl(sb_boolean *b)
             cudaMemcpyAsync(g.newV + 3 * (size_t)A.nv, B.v, sizeof(double) * 3 * B.nv, cudaMemcpyDeviceToDevice, s));
     launch_weld_number(g, (int)nSeq, s);
     if (nTri > 0)
-        k_tri_mesh<<<blocks(nTri, 256), 256, 0, s>>>(nTri, cnts[0], cnts[1], cnts[2], g.triMesh, g.isUncut);
+        SB_COUNT(k_tri_mesh)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, cnts[0], cnts[1], cnts[2], g.triMesh, g.isUncut);
     launch_arrangement(g, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[4], s));
@@ -685,19 +722,19 @@ sb_status combine_impl(sb_boolean *b)
     g.repOfRoot = (int *)(gb + o_ror);
     g.reps = (int *)(gb + o_rep);
     g.insideCount = (int *)(gb + o_ins);
-    k_fill_u64<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeKeys, kEmpty64);
-    k_fill_i32<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeVals, INT_MAX);
+    SB_COUNT(k_fill_u64)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeKeys, kEmpty64);
+    SB_COUNT(k_fill_i32)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeVals, INT_MAX);
     SB_CUDA_CHECK(cudaMemsetAsync(g.degree, 0, sizeof(int) * (nNew + 1), s));
     launch_loops(g, s);
-    k_fill_u64<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysA, kEmpty64);
-    k_fill_u64<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysB, kEmpty64);
-    k_fill_i32<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsA, INT_MAX);
-    k_fill_i32<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsB, INT_MAX);
+    SB_COUNT(k_fill_u64)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysA, kEmpty64);
+    SB_COUNT(k_fill_u64)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysB, kEmpty64);
+    SB_COUNT(k_fill_i32)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsA, INT_MAX);
+    SB_COUNT(k_fill_i32)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsB, INT_MAX);
     if (nTri > 0) {
-        k_iota<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.parent);
-        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.seedMin, INT_MAX);
-        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.remMin, INT_MAX);
-        k_fill_i32<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.repOfRoot, -1);
+        SB_COUNT(k_iota)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.parent);
+        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.seedMin, INT_MAX);
+        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.remMin, INT_MAX);
+        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.repOfRoot, -1);
         SB_CUDA_CHECK(cudaMemsetAsync(g.insideCount, 0, sizeof(int) * (nTri + 1), s));
     }
     launch_groups(g, s);
@@ -806,6 +843,54 @@ const char *sb_status_string(sb_status s)
 
 const char *sb_last_error(void) { return g_last_error.c_str(); }
 
+uint64_t sb_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+void sb_kernel_timing(int enable)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    g_kt_used = 0;
+    g_kt_on.store(enable != 0);
+}
+
+int sb_kernel_timing_read(const char *name, double *total_ms, uint64_t *launches)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    double tot = 0.0;
+    uint64_t n = 0;
+    for (size_t i = 0; i < g_kt_used; ++i) {
+        if (g_kt_recs[i].name != name)
+            continue;
+        if (cudaEventSynchronize(g_kt_recs[i].b) != cudaSuccess)
+            return -1;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, g_kt_recs[i].a, g_kt_recs[i].b) != cudaSuccess)
+            return -1;
+        tot += ms;
+        ++n;
+    }
+    if (total_ms)
+        *total_ms = tot;
+    if (launches)
+        *launches = n;
+    return 0;
+}
+
+int sb_kernel_timing_names(char *buf, size_t cap)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    std::string all;
+    for (size_t i = 0; i < g_kt_used; ++i) {
+        const std::string &n = g_kt_recs[i].name;
+        if (("," + all + ",").find("," + n + ",") == std::string::npos)
+            all += (all.empty() ? "" : ",") + n;
+    }
+    if (buf && cap) {
+        std::strncpy(buf, all.c_str(), cap - 1);
+        buf[cap - 1] = 0;
+    }
+    return (int)all.size();
+}
+
 static sb_status mesh_alloc(size_t nv, size_t nt, sb_mesh **out)
 {
     if (!out || nv > 0x7FFFFFFFu || nt > 0x2AAAAAAAu) {
@@ -837,7 +922,7 @@ static sb_status mesh_validate(sb_mesh *m, cudaStream_t s)
     SB_CUDA_CHECK(m->tmp.ensure(256));
     d_bad = m->tmp.as<unsigned int>();
     SB_CUDA_CHECK(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), s));
-    k_validate_tris<<<blocks(3 * (size_t)m->d.nt, 256), 256, 0, s>>>(m->d.nt, m->d.nv, m->d.t, d_bad);
+    SB_COUNT(k_validate_tris)<<<blocks(3 * (size_t)m->d.nt, 256), 256, 0, s>>>(m->d.nt, m->d.nv, m->d.t, d_bad);
     unsigned int bad = 0;
     SB_CUDA_CHECK(cudaMemcpyAsync(&bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
@@ -1051,7 +1136,7 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
         sz = sizeof(uint32_t) * 2 * (size_t)b->C;
         if (out && sz) {
             SB_CUDA_CHECK(tmp.ensure(sz));
-            k_cand_pairs<<<blocks(b->C, 256), 256, 0, b->s>>>(b->C, b->d_cand, b->second->d.nt, tmp.as<uint32_t>());
+            SB_COUNT(k_cand_pairs)<<<blocks(b->C, 256), 256, 0, b->s>>>(b->C, b->d_cand, b->second->d.nt, tmp.as<uint32_t>());
             SB_CUDA_CHECK(cudaStreamSynchronize(b->s));
             src = tmp.ptr;
         }

@@ -197,7 +197,13 @@ __device__ __forceinline__ double ord_to_dbl(uint64_t u)
 
 } // namespace sbg
 
-#define SB_CUDA_CHECK(expr)                                                                                  \
+namespace sbg {
+// every kernel launch of this library goes through SB_COUNT so the number of launches can be reported
+void count_launch();
+} // namespace sbg
+#define SB_COUNT(kernel) (::sbg::count_launch(), &kernel)
+
+#define SB_CUDA_CHECK(expr)                                                                               \
     do {                                                                                                     \
         cudaError_t _e = (expr);                                                                             \
         if (_e != cudaSuccess)                                                                               \

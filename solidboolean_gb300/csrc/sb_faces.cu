@@ -19,6 +19,7 @@
 #include "sb_common.cuh"
 #include "sb_earcut.cuh"
 #include "sb_faces.cuh"
+#include "sb_ktime.h"
 
 namespace sbg {
 
@@ -637,14 +638,15 @@ void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scr
 {
     if (nFaces <= 0)
         return;
-    k_face_sizes<<<(nFaces + 255) / 256, 256, 0, s>>>(nFaces, faceBegin, scratchBytes, ptCap, triCap, edgeCap);
+    SB_COUNT(k_face_sizes)<<<(nFaces + 255) / 256, 256, 0, s>>>(nFaces, faceBegin, scratchBytes, ptCap, triCap, edgeCap);
 }
 
 void launch_faces(const FaceArgs &a, cudaStream_t s)
 {
     if (a.nFaces <= 0)
         return;
-    k_faces<<<(a.nFaces + 63) / 64, 64, 0, s>>>(a);
+    KTime kt("k_faces", s);
+    SB_COUNT(k_faces)<<<(a.nFaces + 63) / 64, 64, 0, s>>>(a);
 }
 
 } // namespace sbg

@@ -17,6 +17,7 @@
 
 #include "sb_common.cuh"
 #include "sb_internal.h"
+#include "sb_ktime.h"
 #include "sb_pairs.cuh"
 
 namespace cg = cooperative_groups;
@@ -178,6 +179,8 @@ void launch_broad(bool fp64, const MeshDev &A, const MeshDev &B, uint64_t *out, 
     if (A.nt <= 0)
         return;
     int bs = 128, g = (A.nt + bs - 1) / bs;
+    KTime kt("k_broad", s);
+    count_launch();
     if (fp64)
         k_broad<true><<<g, bs, 0, s>>>(A, B, out, count, cap, stats);
     else
@@ -190,6 +193,8 @@ void launch_narrow(bool fp64, const MeshDev &A, const MeshDev &B, const uint64_t
     if (n <= 0)
         return;
     int bs = 128, g = (n + bs - 1) / bs;
+    KTime kt("k_narrow", s);
+    count_launch();
     if (fp64)
         k_narrow<true><<<g, bs, 0, s>>>(A, B, cand, n, hit, seg, stats);
     else

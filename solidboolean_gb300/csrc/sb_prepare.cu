@@ -284,18 +284,18 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     int *idxIn = reinterpret_cast<int *>(tb + t_idx);
 
     const int BS = 256;
-    k_vertices_f32<<<blocks_for(d.nv, BS), BS, 0, s>>>(d.nv, d.v, d.vf);
+    SB_COUNT(k_vertices_f32)<<<blocks_for(d.nv, BS), BS, 0, s>>>(d.nv, d.v, d.vf);
     unsigned int initB[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
     SB_CUDA_CHECK(cudaMemcpyAsync(bounds, initB, sizeof initB, cudaMemcpyHostToDevice, s));
-    k_tri_boxes<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.v, d.t, d.box64, d.box32, cen, bounds);
-    k_morton<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
+    SB_COUNT(k_tri_boxes)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.v, d.t, d.box64, d.box32, cen, bounds);
+    SB_COUNT(k_morton)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tb + t_cub, sortBytes, keyIn, d.morton, idxIn, d.leafTri, nt, 0,
                                                   30, s));
     if (nt > 1) {
         SB_CUDA_CHECK(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * 2 * (size_t)nt, s));
         SB_CUDA_CHECK(cudaMemsetAsync(d.flags, 0, sizeof(int) * (size_t)(nt - 1), s));
-        k_karras<<<blocks_for(nt - 1, BS), BS, 0, s>>>(nt, d.morton, d.child, d.parent);
-        k_refit<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.leafTri, d.box64, d.child, d.parent, d.flags, d.nbox64,
+        SB_COUNT(k_karras)<<<blocks_for(nt - 1, BS), BS, 0, s>>>(nt, d.morton, d.child, d.parent);
+        SB_COUNT(k_refit)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.leafTri, d.box64, d.child, d.parent, d.flags, d.nbox64,
                                                   d.nbox32);
         d.root = 0;
     } else {
