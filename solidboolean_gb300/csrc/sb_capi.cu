@@ -1155,6 +1155,10 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
     } else if (n == "tri_mesh") {
         sz = (size_t)b->nTri;
         src = b->d_triMesh;
+    } else if (n == "rank_first" || n == "rank_second") {
+        const MeshDev &M = n == "rank_first" ? b->first->d : b->second->d;
+        sz = M.rankValid ? sizeof(int) * (size_t)M.nt : 0;
+        src = M.rank;
     } else {
         return SB_ERR_INVALID;
     }

@@ -1,11 +1,338 @@
-// Reference-tree leaf order (placeholder until the GPU top-down build lands).
+// Leaf order of the reference's AABB tree, built on the GPU.
+//
+// The reference's candidate pairs reach each cut face in the order of its tree traversal, and that order
+// numbers the face's cut points (src/solidboolean.cpp:315-341), which in turn decides where closed inner
+// loops start and so how they are ear-clipped, which point of a weld class survives, and whether a face
+// fails. For a fixed first-mesh triangle the dual traversal (src/axisalignedboundingboxtree.h:54-88)
+// visits second-mesh leaves in that tree's left-to-right order (a split of the first tree never reorders
+// the second), and inside a leaf pair in the leaf's stored order. So the per-face order is the position of
+// the other triangle in the other mesh's leaf order, which is what this file computes.
+//
+// The tree (src/axisalignedboundingboxtree.cpp:27-45, 71-141): a node with more than 20 boxes splits on the
+// longest axis of its box (spans compared as float, first maximum wins) at the mean of its box centres
+// (sequential sum in member order divided by (float)count); boxes with centre < mean go left in reverse
+// order of appearance, the others right in order; an empty side takes half of the other.
+//
+// Built level by level: every node's members are a contiguous segment of one permutation. The mean is
+// needed exactly only through the comparisons centre < mean. Each node's sum is accumulated in parallel
+// with a rigorous bound on its distance to the sequential sum (2 gamma_n sum|c|), giving an interval that
+// contains the reference's mean; a member outside the interval is classified exactly, and a node with any
+// member inside it recomputes the sequential sum in member order (one thread) before classifying.
+#include <cub/cub.cuh>
+
 #include "sb_common.cuh"
 #include "sb_internal.h"
 
 namespace sbg {
-sb_status build_reference_rank(sb_mesh *m, cudaStream_t)
+
+struct RNode {
+    int begin, count;
+    int axis, leftFinal, child; // child: id of the left child (right = child + 1), -1 for a leaf
+    int ambiguous;
+    double clo, chi;            // interval holding the reference's split value on `axis`
+    unsigned long long lo[3], hi[3]; // box (order-preserving integer encoding of doubles)
+    double sum[3], asum[3];          // approximate sum of member centres and of their magnitudes
+};
+
+__device__ __forceinline__ void rnode_init(RNode &n, int begin, int count)
 {
-    m->d.rankValid = false;
+    n.begin = begin;
+    n.count = count;
+    n.axis = 0;
+    n.leftFinal = 0;
+    n.child = -1;
+    n.ambiguous = 0;
+    n.clo = n.chi = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        n.lo[k] = ~0ull;
+        n.hi[k] = 0ull;
+        n.sum[k] = 0.0;
+        n.asum[k] = 0.0;
+    }
+}
+
+// box centre of each triangle, exactly as AxisAlignedBoudingBox::updateCenter computes it
+// (((0 + v0) + v1) + v2) / (float)3 (src/axisalignedboundingbox.h:31-53)
+__global__ void k_rr_centres(int nt, const double *__restrict__ v, const uint32_t *__restrict__ t, double *cen,
+                             int *perm, int *nodeOf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt)
+        return;
+    for (int a = 0; a < 3; ++a) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k)
+            s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
+        cen[3 * (size_t)i + a] = s / 3.0;
+    }
+    perm[i] = i;
+    nodeOf[i] = 0;
+}
+
+// adds the members of node `node` (positions p) into that node's box and sums, one atomic per warp when
+// the whole warp belongs to the same node
+__device__ __forceinline__ void rr_accumulate(RNode *nodes, int node, const double *c, const double *bx)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    unsigned mask = __activemask();
+    int lead = __shfl_sync(mask, node, __ffs(mask) - 1);
+    bool uniform = (mask == full) && __all_sync(full, node == lead);
+    unsigned long long lo[3], hi[3];
+    double s[3], as[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = dbl_to_ord(bx[k]);
+        hi[k] = dbl_to_ord(bx[3 + k]);
+        s[k] = c[k];
+        as[k] = fabs(c[k]);
+    }
+    if (uniform) {
+        for (int o = 16; o > 0; o >>= 1)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = min(lo[k], __shfl_xor_sync(full, lo[k], o));
+                hi[k] = max(hi[k], __shfl_xor_sync(full, hi[k], o));
+                s[k] += __shfl_xor_sync(full, s[k], o);
+                as[k] += __shfl_xor_sync(full, as[k], o);
+            }
+        if ((threadIdx.x & 31) != 0)
+            return;
+    }
+    RNode &n = nodes[node];
+    for (int k = 0; k < 3; ++k) {
+        atomicMin(&n.lo[k], lo[k]);
+        atomicMax(&n.hi[k], hi[k]);
+        atomicAdd(&n.sum[k], s[k]);
+        atomicAdd(&n.asum[k], as[k]);
+    }
+}
+
+__global__ void k_rr_root(int nt, const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt)
+        return;
+    rr_accumulate(nodes, 0, cen + 3 * (size_t)i, box64 + 6 * (size_t)i);
+}
+
+// gamma_n = n u / (1 - n u), rounded up
+__device__ __forceinline__ double rr_gamma(int n)
+{
+    const double u = 1.1102230246251565e-16;
+    double nu = __dmul_ru((double)n, u);
+    return __ddiv_ru(nu, __dsub_rd(1.0, nu));
+}
+
+__global__ void k_rr_prep(int first, int last, RNode *nodes, int *nLeafNodes)
+{
+    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= last)
+        return;
+    RNode &n = nodes[id];
+    if (n.count <= 20) {
+        n.child = -1;
+        atomicAdd(nLeafNodes, 1);
+        return;
+    }
+    float span[3];
+    for (int k = 0; k < 3; ++k)
+        span[k] = __double2float_rn(ord_to_dbl(n.hi[k]) - ord_to_dbl(n.lo[k]));
+    int axis = 0;
+    for (int k = 1; k < 3; ++k)
+        if (span[axis] < span[k])
+            axis = k;
+    n.axis = axis;
+    // |sequential - approximate| <= 2 gamma_n sum|c|, with sum|c| itself known to within gamma_n
+    double g = rr_gamma(n.count + 1);
+    double aup = __dmul_ru(n.asum[axis], __dadd_ru(1.0, __dmul_ru(2.0, g)));
+    double err = __dmul_ru(__dmul_ru(2.0, g), aup);
+    err = __dadd_ru(err, 1e-300);
+    double cnt = (double)(float)n.count;
+    n.clo = __ddiv_rd(__dsub_rd(n.sum[axis], err), cnt);
+    n.chi = __ddiv_ru(__dadd_ru(n.sum[axis], err), cnt);
+    n.ambiguous = 0;
+}
+
+// flag: 1 = left, 0 = right; positions of leaves are left untouched (flag 0)
+__global__ void k_rr_classify(int nt, int first, const int *__restrict__ perm, const int *__restrict__ nodeOf,
+                              const double *__restrict__ cen, RNode *nodes, int *flag)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt)
+        return;
+    int id = nodeOf[p];
+    int f = 0;
+    if (id >= first) {
+        RNode &n = nodes[id];
+        if (n.count > 20) {
+            double c = cen[3 * (size_t)perm[p] + n.axis];
+            if (c < n.clo)
+                f = 1;
+            else if (!(c >= n.chi))
+                atomicOr(&n.ambiguous, 1);
+        }
+    }
+    flag[p] = f;
+}
+
+// nodes whose interval could not decide every member: the reference's sequential sum, in member order
+__global__ void k_rr_resolve(int first, int last, const int *__restrict__ perm, const double *__restrict__ cen,
+                             RNode *nodes, int *flag)
+{
+    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= last)
+        return;
+    RNode &n = nodes[id];
+    if (n.count <= 20 || !n.ambiguous)
+        return;
+    double s = 0.0;
+    for (int p = n.begin; p < n.begin + n.count; ++p)
+        s = s + cen[3 * (size_t)perm[p] + n.axis];
+    double split = s / (double)(float)n.count;
+    for (int p = n.begin; p < n.begin + n.count; ++p)
+        flag[p] = cen[3 * (size_t)perm[p] + n.axis] < split ? 1 : 0;
+}
+
+__global__ void k_rr_children(int first, int last, const int *__restrict__ scan, RNode *nodes, int *nodeCount,
+                              int maxNodes)
+{
+    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= last)
+        return;
+    RNode &n = nodes[id];
+    if (n.count <= 20)
+        return;
+    int left = scan[n.begin + n.count] - scan[n.begin];
+    int right = n.count - left;
+    int leftFinal = left;
+    if (left == 0)
+        leftFinal = right / 2;
+    else if (right == 0)
+        leftFinal = left - left / 2;
+    int c = atomicAdd(nodeCount, 2);
+    if (c + 2 > maxNodes) {
+        // out of node records: nothing is written, the host reports a capacity error
+        n.count = 0;
+        atomicAdd(nodeCount + 3, 1);
+        return;
+    }
+    n.leftFinal = leftFinal;
+    n.child = c;
+    rnode_init(nodes[c], n.begin, leftFinal);
+    rnode_init(nodes[c + 1], n.begin + leftFinal, n.count - leftFinal);
+}
+
+__global__ void k_rr_scatter(int nt, int first, const int *__restrict__ perm, const int *__restrict__ nodeOf,
+                             const int *__restrict__ flag, const int *__restrict__ scan, const RNode *nodes,
+                             int *perm2, int *nodeOf2)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt)
+        return;
+    int id = nodeOf[p];
+    if (id < first || nodes[id].count <= 20) {
+        perm2[p] = perm[p];
+        nodeOf2[p] = -1; // settled in a leaf
+        return;
+    }
+    const RNode &n = nodes[id];
+    int left = scan[n.begin + n.count] - scan[n.begin];
+    int lrank = scan[p] - scan[n.begin];
+    int rrank = (p - n.begin) - lrank;
+    int pos;
+    if (left == 0)
+        pos = rrank;
+    else if (left == n.count)
+        pos = n.count - 1 - lrank;
+    else
+        pos = flag[p] ? (left - 1 - lrank) : (left + rrank);
+    int q = n.begin + pos;
+    perm2[q] = perm[p];
+    nodeOf2[q] = pos < n.leftFinal ? n.child : n.child + 1;
+}
+
+__global__ void k_rr_child_stats(int nt, const int *__restrict__ perm, const int *__restrict__ nodeOf,
+                                 const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nt)
+        return;
+    int id = nodeOf[p];
+    if (id < 0)
+        return;
+    int t = perm[p];
+    rr_accumulate(nodes, id, cen + 3 * (size_t)t, box64 + 6 * (size_t)t);
+}
+
+__global__ void k_rr_rank(int nt, const int *__restrict__ perm, int *rank)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nt)
+        rank[perm[p]] = p;
+}
+
+__global__ void k_rr_init_root(RNode *nodes, int nt)
+{
+    rnode_init(nodes[0], 0, nt);
+}
+
+sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
+{
+    MeshDev &d = m->d;
+    const int nt = d.nt;
+    d.rankValid = false;
+    if (nt <= 0)
+        return SB_OK;
+    const int maxNodes = 2 * (nt / 4 + 8) + 64;
+    size_t scanBytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int *)nullptr, (int *)nullptr, nt + 1, s);
+    Carve c;
+    size_t o_cen = c.take<double>(3 * (size_t)nt);
+    size_t o_p1 = c.take<int>(nt), o_p2 = c.take<int>(nt), o_n1 = c.take<int>(nt), o_n2 = c.take<int>(nt);
+    size_t o_fl = c.take<int>(nt + 1), o_sc = c.take<int>(nt + 1);
+    size_t o_nd = c.take<RNode>(maxNodes), o_ct = c.take<int>(4), o_cub = c.take<char>(scanBytes);
+    SB_CUDA_CHECK(m->tmp.ensure(c.off));
+    char *b = m->tmp.as<char>();
+    double *cen = (double *)(b + o_cen);
+    int *perm = (int *)(b + o_p1), *perm2 = (int *)(b + o_p2), *nodeOf = (int *)(b + o_n1), *nodeOf2 = (int *)(b + o_n2);
+    int *flag = (int *)(b + o_fl), *scan = (int *)(b + o_sc);
+    RNode *nodes = (RNode *)(b + o_nd);
+    int *counters = (int *)(b + o_ct); // [0] node count, [1] leaf nodes
+    const int BS = 256, G = (nt + BS - 1) / BS;
+    SB_COUNT(k_rr_centres)<<<G, BS, 0, s>>>(nt, d.v, d.t, cen, perm, nodeOf);
+    SB_COUNT(k_rr_init_root)<<<1, 1, 0, s>>>(nodes, nt);
+    SB_COUNT(k_rr_root)<<<G, BS, 0, s>>>(nt, cen, d.box64, nodes);
+    int one[4] = {1, 0, 0, 0};
+    SB_CUDA_CHECK(cudaMemcpyAsync(counters, one, sizeof one, cudaMemcpyHostToDevice, s));
+    SB_CUDA_CHECK(cudaMemsetAsync(flag + nt, 0, sizeof(int), s));
+    int first = 0, last = 1;
+    for (int level = 0; level < 4096 && first < last; ++level) {
+        const int nl = last - first, GL = (nl + 127) / 128;
+        SB_COUNT(k_rr_prep)<<<GL, 128, 0, s>>>(first, last, nodes, counters + 1);
+        SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, first, perm, nodeOf, cen, nodes, flag);
+        SB_COUNT(k_rr_resolve)<<<GL, 128, 0, s>>>(first, last, perm, cen, nodes, flag);
+        SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
+        SB_COUNT(k_rr_children)<<<GL, 128, 0, s>>>(first, last, scan, nodes, counters, maxNodes);
+        SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, first, perm, nodeOf, flag, scan, nodes, perm2, nodeOf2);
+        SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, perm2, nodeOf2, cen, d.box64, nodes);
+        std::swap(perm, perm2);
+        std::swap(nodeOf, nodeOf2);
+        int cnt[4] = {0, 0, 0, 0};
+        SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        if (cnt[3] != 0) {
+            set_last_error("reference tree node capacity exceeded");
+            return SB_ERR_CAPACITY;
+        }
+        first = last;
+        last = cnt[0];
+    }
+    if (first < last) {
+        set_last_error("reference tree deeper than 4096 levels");
+        return SB_ERR_CAPACITY;
+    }
+    SB_COUNT(k_rr_rank)<<<G, BS, 0, s>>>(nt, perm, d.rank);
+    SB_CUDA_CHECK(cudaGetLastError());
+    d.rankValid = true;
     return SB_OK;
 }
+
 } // namespace sbg

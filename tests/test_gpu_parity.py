@@ -25,3 +25,28 @@ def test_parity(gpu_lib, port, case, precision):
     got = sbg.run_boolean(va, fa, vb, fb, 100000, precision)
     bad = compare(ref, got, len(va) + len(vb), 100000)
     assert not bad, (case, precision, bad, got["stats"])
+
+
+@pytest.mark.parametrize("case", ["pair_small", "pair_large_L5", "near_tangent_L5", "batch"])
+def test_reference_leaf_order(gpu_lib, port, case):
+    """The GPU-built leaf order of the reference tree equals the oracle's, triangle for triangle."""
+    if case == "pair_small":
+        va, fa, vb, fb = mg.pair_small(1234)
+    elif case == "pair_large_L5":
+        va, fa, vb, fb = mg.pair_large(1234, level=5)
+    elif case == "near_tangent_L5":
+        va, fa, vb, fb = mg.near_tangent(1234, level=5)
+    else:
+        va, fa, vb, fb, _ = mg.batch_pair(mg.SplitMix64(11), 5)
+    ref = port.run(va, fa, vb, fb, 100000)
+    opts = sbg.make_options(100000, "filtered", "reference")
+    a, b = sbg.SolidMesh(opts), sbg.SolidMesh(opts)
+    a.setVertices(va), a.setTriangles(fa), b.setVertices(vb), b.setTriangles(fb)
+    a.prepare(), b.prepare()
+    x = sbg.SolidBoolean(a, b, opts)
+    x.combine()
+    for side in ("a", "b"):
+        rank = x.dump("rank_first" if side == "a" else "rank_second", np.int32, 1)
+        order = np.empty_like(rank)
+        order[rank] = np.arange(len(rank), dtype=np.int32)
+        assert np.array_equal(order, ref[f"leaforder_{side}"].astype(np.int32)), side

@@ -1,0 +1,53 @@
+"""Parity on the benchmark-sized workloads and on sampled pairs of the batched workload (mixed
+subdivision levels, so faces with closed inner loops and failing pairs occur)."""
+import numpy as np
+import pytest
+
+import solidboolean_gb300 as sbg
+from solidboolean_gb300 import meshgen as mg
+from parity import compare
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(port, va, fa, vb, fb, q, precision="filtered"):
+    ref = port.run(va, fa, vb, fb, q)
+    got = sbg.run_boolean(va, fa, vb, fb, q, precision)
+    bad = compare(ref, got, len(va) + len(vb), q)
+    assert not bad, (bad, got["stats"])
+    return ref, got
+
+
+def test_pair_large_L7_fine_weld(gpu_lib, port):
+    """327,680 x 327,680 triangles at weld factor 1e8: the full pipeline, bit-exact."""
+    va, fa, vb, fb = mg.pair_large(1234, 7)
+    ref, got = _check(port, va, fa, vb, fb, 100000000)
+    assert ref["status"] == 1
+
+
+def test_pair_large_L7_reference_weld_fails_like_reference(gpu_lib, port):
+    """At the reference's default weld factor the reference fails on this workload; so must we, with the
+    same candidate and intersecting pairs."""
+    va, fa, vb, fb = mg.pair_large(1234, 7)
+    ref, got = _check(port, va, fa, vb, fb, 100000)
+    assert ref["status"] == 0 and got["code"] in (sbg.SB_FAIL_ATTACH, sbg.SB_FAIL_LINK, sbg.SB_FAIL_LOOP)
+
+
+def test_near_tangent_L6(gpu_lib, port):
+    va, fa, vb, fb = mg.near_tangent(1234, 6)
+    _check(port, va, fa, vb, fb, 100000)
+
+
+def test_diff_volume_L5_with_offsets(gpu_lib, port):
+    va, fa, vb, fb, off = mg.diff_volume(1234, 5)
+    _check(port, va, fa, vb + off, fb, 100000)
+
+
+@pytest.mark.parametrize("precision", ["filtered", "fp64"])
+def test_batch_sample(gpu_lib, port, precision):
+    rng = mg.SplitMix64(99)
+    fails = 0
+    for i in range(24):
+        va, fa, vb, fb, _ = mg.batch_pair(rng, 5)
+        ref, got = _check(port, va, fa, vb, fb, 100000, precision)
+        fails += ref["status"] == 0
