@@ -183,6 +183,7 @@ __host__ __device__ inline void hash_iteration_order(const uint64_t *keys, int n
         order[k++] = p;
 }
 
+#ifdef __CUDACC__
 // order-preserving map from double to uint64 (for integer min/max of doubles)
 __device__ __forceinline__ uint64_t dbl_to_ord(double d)
 {
@@ -194,6 +195,7 @@ __device__ __forceinline__ double ord_to_dbl(uint64_t u)
     u = (u & 0x8000000000000000ull) ? (u & 0x7FFFFFFFFFFFFFFFull) : ~u;
     return __longlong_as_double((long long)u);
 }
+#endif
 
 } // namespace sbg
 

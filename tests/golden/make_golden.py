@@ -1,0 +1,84 @@
+"""Generates the golden fixtures from the reference itself (oracle/_ref, compiled from the reference
+sources by oracle/Makefile). Run here, where the reference sources exist:
+
+    python tests/golden/make_golden.py
+
+Each fixture stores the input meshes (so no generator drift can hide a change) and the reference's dumps.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from solidboolean_gb300 import meshgen as mg  # noqa: E402
+
+KEEP = ["cand", "isect", "seg", "newv", "newt", "groups_a_off", "groups_a", "groups_b_off", "groups_b",
+        "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"]
+
+
+def cases():
+    yield "pair_small_1234", mg.pair_small(1234), 100000
+    yield "near_tangent_L3", mg.near_tangent(1234, level=3), 100000
+    va, fa, vb, fb, off = mg.diff_volume(1234, level=3)
+    yield "diff_volume_L3_offsets", (va, fa, vb + off, fb), 100000
+    rng = mg.SplitMix64(7)
+    picked = {}
+    for i in range(200):
+        va, fa, vb, fb, _ = mg.batch_pair(rng, 3)
+        if len(fa) + len(fb) > 3000:
+            continue
+        ref = oracle.reference().run(va, fa, vb, fb, 100000)
+        key = "ok" if ref["status"] else "fail"
+        if key not in picked:
+            picked[key] = (va, fa, vb, fb)
+        if len(picked) == 2:
+            break
+    for key, m in picked.items():
+        yield f"batch_pair_{key}", m, 100000
+
+
+def main():
+    ref = oracle.reference()
+    assert ref is not None, "the reference sources are needed to generate golden fixtures"
+    for name, (va, fa, vb, fb), q in cases():
+        d = ref.run(va, fa, vb, fb, q)
+        out = {k: d[k] for k in KEEP}
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), va=va, fa=fa, vb=vb, fb=fb, quantum=q,
+                            status=d["status"], **out)
+        print(name, "status", d["status"], "candidates", len(d["cand"]), "triangles", len(d["newt"]))
+    # earcut: random star polygons with holes, reference indices
+    rng = np.random.default_rng(5)
+    polys = []
+    for i in range(40):
+        n = int(rng.integers(3, 120))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        rad = rng.uniform(0.5, 1.0, n)
+        outer = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1)
+        rings = [outer]
+        for h in range(int(rng.integers(0, 3))):
+            m = int(rng.integers(3, 8))
+            a = np.sort(rng.uniform(0, 2 * np.pi, m))
+            c = rng.uniform(-0.15, 0.15, 2)
+            rings.append(np.stack([c[0] + 0.1 * np.cos(a), c[1] + 0.1 * np.sin(a)], 1))
+        polys.append(rings)
+    flat, offs, per, idx_all, idx_off = [], [0], [0], [], [0]
+    for rings in polys:
+        for r in rings:
+            flat.append(r)
+            offs.append(offs[-1] + len(r))
+        per.append(per[-1] + len(rings))
+        idx = ref.earcut(rings)
+        idx_all.append(idx)
+        idx_off.append(idx_off[-1] + len(idx))
+    np.savez_compressed(os.path.join(HERE, "earcut_random.npz"), xy=np.concatenate(flat), ring_off=np.array(offs),
+                        poly_off=np.array(per), idx=np.concatenate(idx_all), idx_off=np.array(idx_off))
+    print("earcut fixtures", len(polys))
+
+
+if __name__ == "__main__":
+    main()
