@@ -314,10 +314,16 @@ __global__ void k_region_rep(int nTri, const int *__restrict__ root, const int *
     if (t >= nTri)
         return;
     int r = root[t];
-    if (seedFlag[t])
-        atomicMin(seedMin + r, t);
-    if (isUncut[t])
-        atomicMin(remMin + r, t);
+    // lanes with the same root reduce first, so a big region costs one atomic per warp, not per triangle
+    unsigned mask = __match_any_sync(__activemask(), r);
+    int sv = (int)__reduce_min_sync(mask, (unsigned)(seedFlag[t] ? t : INT_MAX));
+    int rv = (int)__reduce_min_sync(mask, (unsigned)(isUncut[t] ? t : INT_MAX));
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+        if (sv != INT_MAX)
+            atomicMin(seedMin + r, sv);
+        if (rv != INT_MAX)
+            atomicMin(remMin + r, rv);
+    }
 }
 
 __global__ void k_region_list(int nTri, const int *__restrict__ root, const int *__restrict__ seedMin,
@@ -336,32 +342,45 @@ __global__ void k_region_list(int nTri, const int *__restrict__ root, const int 
     }
 }
 
-// isPointInMesh (src/solidboolean.cpp:48-92) for one (region, axis)
+// isPointInMesh (src/solidboolean.cpp:48-92) for one (region, axis) per warp: the 32 lanes pop up to 32
+// LBVH nodes at a time from a per-warp shared-memory stack, test the children against the ray's box
+// (FP32 boxes rounded outward, or exact FP64 boxes in the plain form), test reached triangles exactly in
+// FP64 (closed-interval box test, plane hit, three same-sign normals) and collect the hit points; the
+// parity of the number of distinct PositionKeys decides the axis.
+constexpr int kSideWarps = 4;
+constexpr int kSideStack = 1536; // per warp; 4 warps x (1536 x 4 B + 128 x 24 B) = 36 KB of static smem
+constexpr int kSideHits = 128;
+
 template <bool FP64>
-__global__ void k_sides(unsigned int nReps, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
-                        const uint32_t *__restrict__ newT, const double *__restrict__ newV,
-                        const int8_t *__restrict__ triMesh, MeshDev A, MeshDev B, double factor, int *insideCount,
-                        unsigned int *errors)
+__global__ void __launch_bounds__(32 * kSideWarps)
+    k_sides(unsigned int nReps, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
+            const uint32_t *__restrict__ newT, const double *__restrict__ newV, const int8_t *__restrict__ triMesh,
+            MeshDev A, MeshDev B, double factor, int *insideCount, unsigned int *errors)
 {
-    unsigned int w = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int stack[kSideWarps][kSideStack];
+    __shared__ Key hits[kSideWarps][kSideHits];
+    __shared__ int spS[kSideWarps], nhS[kSideWarps], errS[kSideWarps];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xFFFFFFFFu;
+    unsigned int w = blockIdx.x * kSideWarps + wl;
     if (w >= 3 * nReps)
         return;
-    int r = reps[w / 3];
-    int axis = (int)(w % 3);
-    int rep = repOfRoot[r];
+    const int r = reps[w / 3];
+    const int axis = (int)(w % 3);
+    const int rep = repOfRoot[r];
     const MeshDev &M = triMesh[rep] == 0 ? B : A; // the other mesh
     const uint32_t *tv = newT + 3 * (size_t)rep;
     d3 v0 = mk(newV[3 * (size_t)tv[0]], newV[3 * (size_t)tv[0] + 1], newV[3 * (size_t)tv[0] + 2]);
     d3 v1 = mk(newV[3 * (size_t)tv[1]], newV[3 * (size_t)tv[1] + 1], newV[3 * (size_t)tv[1] + 2]);
     d3 v2 = mk(newV[3 * (size_t)tv[2]], newV[3 * (size_t)tv[2] + 1], newV[3 * (size_t)tv[2] + 2]);
-    d3 p = divs((v0 + v1) + v2, 3.0);
-    d3 ax = mk(axis == 0 ? kDblMax : kDblEps, axis == 1 ? kDblMax : kDblEps, axis == 2 ? kDblMax : kDblEps);
-    d3 e = p + ax;
+    const d3 p = divs((v0 + v1) + v2, 3.0);
+    const d3 ax = mk(axis == 0 ? kDblMax : kDblEps, axis == 1 ? kDblMax : kDblEps, axis == 2 ? kDblMax : kDblEps);
+    const d3 e = p + ax;
     double qlo[3], qhi[3];
+    float olo[3], ohi[3];
     for (int k = 0; k < 3; ++k) {
         double a = comp(p, k), b = comp(e, k);
-        // AxisAlignedBoudingBox::update with p then e
-        double lo = kDblMax, hi = -kDblMax;
+        double lo = kDblMax, hi = -kDblMax; // AxisAlignedBoudingBox::update with p then e
         if (a > hi)
             hi = a;
         if (a < lo)
@@ -372,16 +391,16 @@ __global__ void k_sides(unsigned int nReps, const int *__restrict__ reps, const 
             lo = b;
         qlo[k] = lo;
         qhi[k] = hi;
+        olo[k] = __double2float_rd(lo);
+        ohi[k] = __double2float_ru(hi);
     }
-    float olo[3], ohi[3];
-    for (int k = 0; k < 3; ++k) {
-        olo[k] = __double2float_rd(qlo[k]);
-        ohi[k] = __double2float_ru(qhi[k]);
+    const d3 u = e - p;
+    if (lane == 0) {
+        spS[wl] = 0;
+        nhS[wl] = 0;
+        errS[wl] = 0;
     }
-    Key hits[64];
-    int nh = 0;
-    bool overflow = false;
-    d3 u = e - p;
+    __syncwarp();
     auto test_tri = [&](int ti) {
         const double *bx = M.box64 + 6 * (size_t)ti;
         for (int k = 0; k < 3; ++k)
@@ -406,24 +425,30 @@ __global__ void k_sides(unsigned int nReps, const int *__restrict__ reps, const 
         d3 n2 = unit_normal(x, tp[2], tp[0]);
         if (!(dot(n0, n1) > 0 && dot(n0, n2) > 0))
             return;
-        Key k = make_key(x, factor);
-        for (int q = 0; q < nh; ++q)
-            if (key_eq(hits[q], k))
-                return;
-        if (nh < 64)
-            hits[nh++] = k;
+        int k = atomicAdd(&nhS[wl], 1);
+        if (k < kSideHits)
+            hits[wl][k] = make_key(x, factor);
         else
-            overflow = true;
+            errS[wl] = 1;
     };
     if (M.nt > 0) {
         if (M.root < 0) {
-            test_tri(M.leafTri[0]);
-        } else {
-            int stack[96];
-            int sp = 0;
-            stack[sp++] = M.root;
-            while (sp > 0) {
-                int node = stack[--sp];
+            if (lane == 0)
+                test_tri(M.leafTri[0]);
+        } else if (lane == 0) {
+            stack[wl][0] = M.root;
+            spS[wl] = 1;
+        }
+        __syncwarp();
+        for (int iter = 0; iter < (1 << 20); ++iter) {
+            int sp = spS[wl];
+            int n = min(sp, 32);
+            if (n == 0)
+                break;
+            int node = lane < n ? stack[wl][sp - n + lane] : -1;
+            __syncwarp();
+            int push[2] = {-1, -1};
+            if (node >= 0) {
                 int2 ch = M.child[node];
                 int cs[2] = {ch.x, ch.y};
                 for (int k = 0; k < 2; ++k) {
@@ -442,20 +467,52 @@ __global__ void k_sides(unsigned int nReps, const int *__restrict__ reps, const 
                         hit = olo[0] <= bx[3] && ohi[0] >= bx[0] && olo[1] <= bx[4] && ohi[1] >= bx[1] &&
                               olo[2] <= bx[5] && ohi[2] >= bx[2];
                     }
-                    if (hit) {
-                        if (sp < 96)
-                            stack[sp++] = c;
-                        else
-                            overflow = true;
-                    }
+                    if (hit)
+                        push[k] = c;
                 }
             }
+            int cnt = (push[0] >= 0) + (push[1] >= 0);
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(full, incl, o);
+                if (lane >= o)
+                    incl += v;
+            }
+            int total = __shfl_sync(full, incl, 31);
+            int base = sp - n;
+            if (base + total > kSideStack) {
+                if (lane == 0)
+                    errS[wl] = 1;
+                break;
+            }
+            int pos = base + incl - cnt;
+            for (int k = 0; k < 2; ++k)
+                if (push[k] >= 0)
+                    stack[wl][pos++] = push[k];
+            __syncwarp();
+            if (lane == 0)
+                spS[wl] = base + total;
+            __syncwarp();
         }
     }
-    if (overflow)
-        atomicAdd(errors, 1u);
-    if (nh % 2 != 0)
-        atomicAdd(insideCount + r, 1);
+    __syncwarp();
+    // distinct keys among the hits (std::set<PositionKey> in the reference)
+    int nh = min(nhS[wl], kSideHits);
+    int distinct = 0;
+    for (int h = lane; h < nh; h += 32) {
+        bool dup = false;
+        for (int j = 0; j < h && !dup; ++j)
+            dup = key_eq(hits[wl][j], hits[wl][h]);
+        distinct += dup ? 0 : 1;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        distinct += __shfl_xor_sync(full, distinct, o);
+    if (lane == 0) {
+        if (errS[wl])
+            atomicAdd(errors, 1u);
+        if (distinct % 2 != 0)
+            atomicAdd(insideCount + r, 1);
+    }
 }
 
 __global__ void k_labels(int nTri, const int *__restrict__ root, const int *__restrict__ repOfRoot,
@@ -631,11 +688,11 @@ void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t 
         KTime kt("k_sides", s);
         count_launch();
         if (fp64)
-            k_sides<true><<<nb(3 * (size_t)nReps, 64), 64, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
+            k_sides<true><<<nb(3 * (size_t)nReps, kSideWarps), 32 * kSideWarps, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
                                                                    g.triMesh, g.A, g.B, g.factor, g.insideCount,
                                                                    g.counters + kCntSideErrors);
         else
-            k_sides<false><<<nb(3 * (size_t)nReps, 64), 64, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
+            k_sides<false><<<nb(3 * (size_t)nReps, kSideWarps), 32 * kSideWarps, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
                                                                     g.triMesh, g.A, g.B, g.factor, g.insideCount,
                                                                     g.counters + kCntSideErrors);
     }
