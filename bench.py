@@ -207,8 +207,10 @@ def gpu_arm(args, rank, world, local, dist):
         stats = sbg.Stats()
 
         def step():
-            sbg._check(L.sb_mesh_prepare(hA, ctypes.byref(opts)), "prepare A")
-            sbg._check(L.sb_mesh_prepare(hB, ctypes.byref(opts)), "prepare B")
+            # fresh vertex upload marks both meshes unprepared; combine() then rebuilds both meshes'
+            # acceleration structures (concurrently, on two streams) before the boolean itself
+            sbg._check(L.sb_mesh_update_vertices_device(hA, tv[0].data_ptr(), ctypes.byref(opts)), "update A")
+            sbg._check(L.sb_mesh_update_vertices_device(hB, tv[1].data_ptr(), ctypes.byref(opts)), "update B")
             code = sbg._check(L.sb_combine(hX, ctypes.byref(stats)), "combine")
             return code
 

@@ -9,6 +9,7 @@
 #include <climits>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -277,6 +278,8 @@ struct sb_boolean {
     uint32_t *d_fetch[3] = {nullptr, nullptr, nullptr};
     size_t nFetch[3] = {0, 0, 0};
     cudaEvent_t ev[10];
+    cudaStream_t side = nullptr;     // second stream for preparing the two meshes concurrently
+    cudaEvent_t sideDone = nullptr;
     bool evInit = false;
     unsigned int *h_pinned = nullptr; // host mirror of small counters
 };
@@ -1040,9 +1043,30 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
     if (!b)
         return SB_ERR_INVALID;
     return guarded([&]() -> sb_status {
-        for (const sb_mesh *m : {b->first, b->second})
+        sb_mesh *ma = const_cast<sb_mesh *>(b->first), *mb = const_cast<sb_mesh *>(b->second);
+        if (!ma->prepared && !mb->prepared && ma != mb) {
+            // both meshes need preparing: the second one on a side stream from a helper thread, so the two
+            // latency-bound builds overlap; the main stream then waits for the side stream
+            if (!b->side) {
+                SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+                SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->sideDone, cudaEventDisableTiming));
+            }
+            SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->s));
+            SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
+            sb_status rb = SB_OK;
+            std::thread helper([&]() { rb = prepare_mesh(mb, b->opts.order, b->side); });
+            sb_status ra = prepare_mesh(ma, b->opts.order, b->s);
+            helper.join();
+            if (ra != SB_OK)
+                return ra;
+            if (rb != SB_OK)
+                return rb;
+            SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->side));
+            SB_CUDA_CHECK(cudaStreamWaitEvent(b->s, b->sideDone, 0));
+        }
+        for (sb_mesh *m : {ma, mb})
             if (!m->prepared) {
-                sb_status r = prepare_mesh(const_cast<sb_mesh *>(m), b->opts.order, b->s);
+                sb_status r = prepare_mesh(m, b->opts.order, b->s);
                 if (r != SB_OK)
                     return r;
             }
@@ -1188,6 +1212,10 @@ void sb_boolean_destroy(sb_boolean *b)
     if (b->evInit)
         for (auto &e : b->ev)
             cudaEventDestroy(e);
+    if (b->side) {
+        cudaStreamDestroy(b->side);
+        cudaEventDestroy(b->sideDone);
+    }
     delete b;
 }
 

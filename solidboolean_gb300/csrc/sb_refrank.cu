@@ -22,6 +22,7 @@
 
 #include "sb_common.cuh"
 #include "sb_internal.h"
+#include "sb_ktime.h"
 
 namespace sbg {
 
@@ -105,12 +106,71 @@ __device__ __forceinline__ void rr_accumulate(RNode *nodes, int node, const doub
     }
 }
 
+// all threads of the block call this; a block whose valid threads all belong to one node reduces in
+// shared memory first (one set of atomics per block), other blocks fall back to warp-level reduction
+__device__ void rr_block_accumulate(RNode *nodes, int node, const double *c, const double *bx)
+{
+    __shared__ int sNode;
+    __shared__ unsigned long long sLo[32][3], sHi[32][3];
+    __shared__ double sSum[32][3], sAbs[32][3];
+    if (threadIdx.x == 0)
+        sNode = node;
+    __syncthreads();
+    const bool uniform = __syncthreads_and(node == sNode) && sNode >= 0;
+    if (!uniform) {
+        if (node >= 0)
+            rr_accumulate(nodes, node, c, bx);
+        return;
+    }
+    const unsigned full = 0xFFFFFFFFu;
+    unsigned long long lo[3], hi[3];
+    double sm[3], as[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = dbl_to_ord(bx[k]);
+        hi[k] = dbl_to_ord(bx[3 + k]);
+        sm[k] = c[k];
+        as[k] = fabs(c[k]);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = min(lo[k], __shfl_xor_sync(full, lo[k], o));
+            hi[k] = max(hi[k], __shfl_xor_sync(full, hi[k], o));
+            sm[k] += __shfl_xor_sync(full, sm[k], o);
+            as[k] += __shfl_xor_sync(full, as[k], o);
+        }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; ++k) {
+            sLo[w][k] = lo[k];
+            sHi[w][k] = hi[k];
+            sSum[w][k] = sm[k];
+            sAbs[w][k] = as[k];
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        unsigned long long l = ~0ull, h = 0ull;
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < nw; ++i) {
+            l = min(l, sLo[i][k]);
+            h = max(h, sHi[i][k]);
+            a += sSum[i][k];
+            b += sAbs[i][k];
+        }
+        RNode &n = nodes[node];
+        atomicMin(&n.lo[k], l);
+        atomicMax(&n.hi[k], h);
+        atomicAdd(&n.sum[k], a);
+        atomicAdd(&n.asum[k], b);
+    }
+}
+
 __global__ void k_rr_root(int nt, const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nt)
-        return;
-    rr_accumulate(nodes, 0, cen + 3 * (size_t)i, box64 + 6 * (size_t)i);
+    int node = i < nt ? 0 : -1;
+    int j = i < nt ? i : 0;
+    rr_block_accumulate(nodes, node, cen + 3 * (size_t)j, box64 + 6 * (size_t)j);
 }
 
 // gamma_n = n u / (1 - n u), rounded up
@@ -121,46 +181,47 @@ __device__ __forceinline__ double rr_gamma(int n)
     return __ddiv_ru(nu, __dsub_rd(1.0, nu));
 }
 
-__global__ void k_rr_prep(int first, int last, RNode *nodes, int *nLeafNodes)
+// bounds[0..1]: first and one-past-last node of the current level; counters[1] counts leaves
+__global__ void k_rr_prep(const int *__restrict__ bounds, RNode *nodes, int *counters)
 {
-    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= last)
-        return;
-    RNode &n = nodes[id];
-    if (n.count <= 20) {
-        n.child = -1;
-        atomicAdd(nLeafNodes, 1);
-        return;
+    const int first = bounds[0], last = bounds[1];
+    for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
+        RNode &n = nodes[id];
+        if (n.count <= 20) {
+            n.child = -1;
+            atomicAdd(counters + 1, 1);
+            continue;
+        }
+        float span[3];
+        for (int k = 0; k < 3; ++k)
+            span[k] = __double2float_rn(ord_to_dbl(n.hi[k]) - ord_to_dbl(n.lo[k]));
+        int axis = 0;
+        for (int k = 1; k < 3; ++k)
+            if (span[axis] < span[k])
+                axis = k;
+        n.axis = axis;
+        // |sequential - approximate| <= 2 gamma_n sum|c|, with sum|c| itself known to within gamma_n
+        double g = rr_gamma(n.count + 1);
+        double aup = __dmul_ru(n.asum[axis], __dadd_ru(1.0, __dmul_ru(2.0, g)));
+        double err = __dmul_ru(__dmul_ru(2.0, g), aup);
+        err = __dadd_ru(err, 1e-300);
+        double cnt = (double)(float)n.count;
+        n.clo = __ddiv_rd(__dsub_rd(n.sum[axis], err), cnt);
+        n.chi = __ddiv_ru(__dadd_ru(n.sum[axis], err), cnt);
+        n.ambiguous = 0;
     }
-    float span[3];
-    for (int k = 0; k < 3; ++k)
-        span[k] = __double2float_rn(ord_to_dbl(n.hi[k]) - ord_to_dbl(n.lo[k]));
-    int axis = 0;
-    for (int k = 1; k < 3; ++k)
-        if (span[axis] < span[k])
-            axis = k;
-    n.axis = axis;
-    // |sequential - approximate| <= 2 gamma_n sum|c|, with sum|c| itself known to within gamma_n
-    double g = rr_gamma(n.count + 1);
-    double aup = __dmul_ru(n.asum[axis], __dadd_ru(1.0, __dmul_ru(2.0, g)));
-    double err = __dmul_ru(__dmul_ru(2.0, g), aup);
-    err = __dadd_ru(err, 1e-300);
-    double cnt = (double)(float)n.count;
-    n.clo = __ddiv_rd(__dsub_rd(n.sum[axis], err), cnt);
-    n.chi = __ddiv_ru(__dadd_ru(n.sum[axis], err), cnt);
-    n.ambiguous = 0;
 }
 
 // flag: 1 = left, 0 = right; positions of leaves are left untouched (flag 0)
-__global__ void k_rr_classify(int nt, int first, const int *__restrict__ perm, const int *__restrict__ nodeOf,
-                              const double *__restrict__ cen, RNode *nodes, int *flag)
+__global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const int *__restrict__ perm,
+                              const int *__restrict__ nodeOf, const double *__restrict__ cen, RNode *nodes, int *flag)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nt)
         return;
     int id = nodeOf[p];
     int f = 0;
-    if (id >= first) {
+    if (id >= bounds[0]) {
         RNode &n = nodes[id];
         if (n.count > 20) {
             double c = cen[3 * (size_t)perm[p] + n.axis];
@@ -174,61 +235,61 @@ __global__ void k_rr_classify(int nt, int first, const int *__restrict__ perm, c
 }
 
 // nodes whose interval could not decide every member: the reference's sequential sum, in member order
-__global__ void k_rr_resolve(int first, int last, const int *__restrict__ perm, const double *__restrict__ cen,
-                             RNode *nodes, int *flag)
+__global__ void k_rr_resolve(const int *__restrict__ bounds, const int *__restrict__ perm,
+                             const double *__restrict__ cen, RNode *nodes, int *flag)
 {
-    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= last)
-        return;
-    RNode &n = nodes[id];
-    if (n.count <= 20 || !n.ambiguous)
-        return;
-    double s = 0.0;
-    for (int p = n.begin; p < n.begin + n.count; ++p)
-        s = s + cen[3 * (size_t)perm[p] + n.axis];
-    double split = s / (double)(float)n.count;
-    for (int p = n.begin; p < n.begin + n.count; ++p)
-        flag[p] = cen[3 * (size_t)perm[p] + n.axis] < split ? 1 : 0;
-}
-
-__global__ void k_rr_children(int first, int last, const int *__restrict__ scan, RNode *nodes, int *nodeCount,
-                              int maxNodes)
-{
-    int id = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= last)
-        return;
-    RNode &n = nodes[id];
-    if (n.count <= 20)
-        return;
-    int left = scan[n.begin + n.count] - scan[n.begin];
-    int right = n.count - left;
-    int leftFinal = left;
-    if (left == 0)
-        leftFinal = right / 2;
-    else if (right == 0)
-        leftFinal = left - left / 2;
-    int c = atomicAdd(nodeCount, 2);
-    if (c + 2 > maxNodes) {
-        // out of node records: nothing is written, the host reports a capacity error
-        n.count = 0;
-        atomicAdd(nodeCount + 3, 1);
-        return;
+    const int first = bounds[0], last = bounds[1];
+    for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
+        RNode &n = nodes[id];
+        if (n.count <= 20 || !n.ambiguous)
+            continue;
+        double s = 0.0;
+        for (int p = n.begin; p < n.begin + n.count; ++p)
+            s = s + cen[3 * (size_t)perm[p] + n.axis];
+        double split = s / (double)(float)n.count;
+        for (int p = n.begin; p < n.begin + n.count; ++p)
+            flag[p] = cen[3 * (size_t)perm[p] + n.axis] < split ? 1 : 0;
     }
-    n.leftFinal = leftFinal;
-    n.child = c;
-    rnode_init(nodes[c], n.begin, leftFinal);
-    rnode_init(nodes[c + 1], n.begin + leftFinal, n.count - leftFinal);
 }
 
-__global__ void k_rr_scatter(int nt, int first, const int *__restrict__ perm, const int *__restrict__ nodeOf,
-                             const int *__restrict__ flag, const int *__restrict__ scan, const RNode *nodes,
-                             int *perm2, int *nodeOf2)
+__global__ void k_rr_children(const int *__restrict__ bounds, const int *__restrict__ scan, RNode *nodes,
+                              int *counters, int maxNodes)
+{
+    const int first = bounds[0], last = bounds[1];
+    for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
+        RNode &n = nodes[id];
+        if (n.count <= 20)
+            continue;
+        int left = scan[n.begin + n.count] - scan[n.begin];
+        int right = n.count - left;
+        int leftFinal = left;
+        if (left == 0)
+            leftFinal = right / 2;
+        else if (right == 0)
+            leftFinal = left - left / 2;
+        int c = atomicAdd(counters, 2);
+        if (c + 2 > maxNodes) {
+            // out of node records: nothing is written, the host reports a capacity error
+            n.count = 0;
+            atomicAdd(counters + 3, 1);
+            continue;
+        }
+        n.leftFinal = leftFinal;
+        n.child = c;
+        rnode_init(nodes[c], n.begin, leftFinal);
+        rnode_init(nodes[c + 1], n.begin + leftFinal, n.count - leftFinal);
+    }
+}
+
+__global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const int *__restrict__ perm,
+                             const int *__restrict__ nodeOf, const int *__restrict__ flag,
+                             const int *__restrict__ scan, const RNode *nodes, int *perm2, int *nodeOf2)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nt)
         return;
     int id = nodeOf[p];
-    if (id < first || nodes[id].count <= 20) {
+    if (id < bounds[0] || nodes[id].count <= 20) {
         perm2[p] = perm[p];
         nodeOf2[p] = -1; // settled in a leaf
         return;
@@ -253,13 +314,16 @@ __global__ void k_rr_child_stats(int nt, const int *__restrict__ perm, const int
                                  const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nt)
-        return;
-    int id = nodeOf[p];
-    if (id < 0)
-        return;
-    int t = perm[p];
-    rr_accumulate(nodes, id, cen + 3 * (size_t)t, box64 + 6 * (size_t)t);
+    int id = p < nt ? nodeOf[p] : -1;
+    int t = id >= 0 ? perm[p] : 0;
+    rr_block_accumulate(nodes, id, cen + 3 * (size_t)t, box64 + 6 * (size_t)t);
+}
+
+// next level: [last, nodes allocated so far)
+__global__ void k_rr_advance(int *bounds, const int *counters)
+{
+    bounds[0] = bounds[1];
+    bounds[1] = counters[0];
 }
 
 __global__ void k_rr_rank(int nt, const int *__restrict__ perm, int *rank)
@@ -269,9 +333,14 @@ __global__ void k_rr_rank(int nt, const int *__restrict__ perm, int *rank)
         rank[perm[p]] = p;
 }
 
-__global__ void k_rr_init_root(RNode *nodes, int nt)
+__global__ void k_rr_init_root(RNode *nodes, int nt, int *counters)
 {
     rnode_init(nodes[0], 0, nt);
+    counters[0] = 1; // nodes allocated
+    counters[1] = 0; // leaves
+    counters[3] = 0; // capacity overflow
+    counters[4] = 0; // level bounds: first
+    counters[5] = 1; //               one past last
 }
 
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
@@ -281,6 +350,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     d.rankValid = false;
     if (nt <= 0)
         return SB_OK;
+    KTime kt("reference_leaf_order", s);
     const int maxNodes = 2 * (nt / 4 + 8) + 64;
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int *)nullptr, (int *)nullptr, nt + 1, s);
@@ -288,44 +358,46 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     size_t o_cen = c.take<double>(3 * (size_t)nt);
     size_t o_p1 = c.take<int>(nt), o_p2 = c.take<int>(nt), o_n1 = c.take<int>(nt), o_n2 = c.take<int>(nt);
     size_t o_fl = c.take<int>(nt + 1), o_sc = c.take<int>(nt + 1);
-    size_t o_nd = c.take<RNode>(maxNodes), o_ct = c.take<int>(4), o_cub = c.take<char>(scanBytes);
+    size_t o_nd = c.take<RNode>(maxNodes), o_ct = c.take<int>(8), o_cub = c.take<char>(scanBytes);
     SB_CUDA_CHECK(m->tmp.ensure(c.off));
     char *b = m->tmp.as<char>();
     double *cen = (double *)(b + o_cen);
     int *perm = (int *)(b + o_p1), *perm2 = (int *)(b + o_p2), *nodeOf = (int *)(b + o_n1), *nodeOf2 = (int *)(b + o_n2);
     int *flag = (int *)(b + o_fl), *scan = (int *)(b + o_sc);
     RNode *nodes = (RNode *)(b + o_nd);
-    int *counters = (int *)(b + o_ct); // [0] node count, [1] leaf nodes
-    const int BS = 256, G = (nt + BS - 1) / BS;
+    int *counters = (int *)(b + o_ct); // [0] nodes, [1] leaves, [3] overflow, [4..5] level bounds
+    int *bounds = counters + 4;
+    const int BS = 256, G = (nt + BS - 1) / BS, GN = 152 * 4;
     SB_COUNT(k_rr_centres)<<<G, BS, 0, s>>>(nt, d.v, d.t, cen, perm, nodeOf);
-    SB_COUNT(k_rr_init_root)<<<1, 1, 0, s>>>(nodes, nt);
+    SB_COUNT(k_rr_init_root)<<<1, 1, 0, s>>>(nodes, nt, counters);
     SB_COUNT(k_rr_root)<<<G, BS, 0, s>>>(nt, cen, d.box64, nodes);
-    int one[4] = {1, 0, 0, 0};
-    SB_CUDA_CHECK(cudaMemcpyAsync(counters, one, sizeof one, cudaMemcpyHostToDevice, s));
     SB_CUDA_CHECK(cudaMemsetAsync(flag + nt, 0, sizeof(int), s));
-    int first = 0, last = 1;
-    for (int level = 0; level < 4096 && first < last; ++level) {
-        const int nl = last - first, GL = (nl + 127) / 128;
-        SB_COUNT(k_rr_prep)<<<GL, 128, 0, s>>>(first, last, nodes, counters + 1);
-        SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, first, perm, nodeOf, cen, nodes, flag);
-        SB_COUNT(k_rr_resolve)<<<GL, 128, 0, s>>>(first, last, perm, cen, nodes, flag);
-        SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
-        SB_COUNT(k_rr_children)<<<GL, 128, 0, s>>>(first, last, scan, nodes, counters, maxNodes);
-        SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, first, perm, nodeOf, flag, scan, nodes, perm2, nodeOf2);
-        SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, perm2, nodeOf2, cen, d.box64, nodes);
-        std::swap(perm, perm2);
-        std::swap(nodeOf, nodeOf2);
-        int cnt[4] = {0, 0, 0, 0};
+    // levels run in batches; the host looks at the level bounds only between batches
+    const int kBatch = 6;
+    bool done = false;
+    for (int level = 0; level < 4096 && !done; level += kBatch) {
+        for (int j = 0; j < kBatch; ++j) {
+            SB_COUNT(k_rr_prep)<<<GN, 128, 0, s>>>(bounds, nodes, counters);
+            SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, bounds, perm, nodeOf, cen, nodes, flag);
+            SB_COUNT(k_rr_resolve)<<<GN, 128, 0, s>>>(bounds, perm, cen, nodes, flag);
+            SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
+            SB_COUNT(k_rr_children)<<<GN, 128, 0, s>>>(bounds, scan, nodes, counters, maxNodes);
+            SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, bounds, perm, nodeOf, flag, scan, nodes, perm2, nodeOf2);
+            SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, perm2, nodeOf2, cen, d.box64, nodes);
+            SB_COUNT(k_rr_advance)<<<1, 1, 0, s>>>(bounds, counters);
+            std::swap(perm, perm2);
+            std::swap(nodeOf, nodeOf2);
+        }
+        int cnt[8];
         SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaStreamSynchronize(s));
         if (cnt[3] != 0) {
             set_last_error("reference tree node capacity exceeded");
             return SB_ERR_CAPACITY;
         }
-        first = last;
-        last = cnt[0];
+        done = cnt[4] >= cnt[5];
     }
-    if (first < last) {
+    if (!done) {
         set_last_error("reference tree deeper than 4096 levels");
         return SB_ERR_CAPACITY;
     }
