@@ -670,7 +670,7 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_L = cr.take<int8_t>(nTri + 1), o_M = cr.take<int8_t>(nTri + 1), o_U = cr.take<int8_t>(nTri + 1);
     size_t o_F0 = cr.take<uint32_t>(3 * (size_t)nTri + 3), o_F1 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
     size_t o_F2 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
-    size_t o_fl = cr.take<int>(nTri + 1), o_fr2 = cr.take<int>(nTri + 1);
+    size_t o_fl = cr.take<int>(3 * ((size_t)nTri + 1)), o_fr2 = cr.take<int>(3 * ((size_t)nTri + 1));
     SB_CUDA_CHECK(b->res.ensure(cr.off));
     char *rb = b->res.as<char>();
     g.newV = (double *)(rb + o_V);
@@ -769,17 +769,22 @@ sb_status combine_impl(sb_boolean *b)
 
     // ---------------- fetch ----------------
     if (status == SB_OK && nTri > 0) {
+        // the three fetch compactions, one host read of their sizes
+        int n[3] = {0, 0, 0};
         for (int op = 0; op < 3; ++op) {
-            launch_fetch_flags(g, op, fFlag, s);
+            int *fl = fFlag + op * ((size_t)nTri + 1), *rk = fRank + op * ((size_t)nTri + 1);
+            SB_CUDA_CHECK(cudaMemsetAsync(fl + nTri, 0, sizeof(int), s));
+            launch_fetch_flags(g, op, fl, s);
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-                return cub::DeviceScan::ExclusiveSum(tmp, bytes, fFlag, fRank, nTri + 1, s);
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, fl, rk, nTri + 1, s);
             }));
-            launch_fetch_write(g, op, fFlag, fRank, fetchOut[op], s);
-            int n = 0;
-            SB_CUDA_CHECK(cudaMemcpyAsync(&n, fRank + nTri, sizeof n, cudaMemcpyDeviceToHost, s));
-            SB_CUDA_CHECK(cudaStreamSynchronize(s));
+            launch_fetch_write(g, op, fl, rk, fetchOut[op], s);
+            SB_CUDA_CHECK(cudaMemcpyAsync(n + op, rk + nTri, sizeof(int), cudaMemcpyDeviceToHost, s));
+        }
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        for (int op = 0; op < 3; ++op) {
             b->d_fetch[op] = fetchOut[op];
-            b->nFetch[op] = (size_t)n;
+            b->nFetch[op] = (size_t)n[op];
         }
     }
     SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));

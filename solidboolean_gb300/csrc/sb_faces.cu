@@ -602,7 +602,7 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f)
     return res;
 }
 
-__global__ void __launch_bounds__(64) k_faces(FaceArgs a)
+__global__ void __launch_bounds__(32) k_faces(FaceArgs a)
 {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= a.nFaces)
@@ -646,7 +646,7 @@ void launch_faces(const FaceArgs &a, cudaStream_t s)
     if (a.nFaces <= 0)
         return;
     KTime kt("k_faces", s);
-    SB_COUNT(k_faces)<<<(a.nFaces + 63) / 64, 64, 0, s>>>(a);
+    SB_COUNT(k_faces)<<<(a.nFaces + 31) / 32, 32, 0, s>>>(a);
 }
 
 } // namespace sbg

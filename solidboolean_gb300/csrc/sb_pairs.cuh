@@ -113,6 +113,29 @@ template <bool FP64> struct TriTri {
         have64 = true;
     }
 
+
+    // register-resident selection of slot i (runtime index into the arrays would spill them to local memory)
+    __device__ __forceinline__ float4 fs(int i) const
+    {
+        float4 r = F[0];
+        r = i == 1 ? F[1] : r;
+        r = i == 2 ? F[2] : r;
+        r = i == 3 ? F[3] : r;
+        r = i == 4 ? F[4] : r;
+        r = i == 5 ? F[5] : r;
+        return r;
+    }
+    __device__ __forceinline__ d3 ps(int i) const
+    {
+        d3 r = P[0];
+        r = i == 1 ? P[1] : r;
+        r = i == 2 ? P[2] : r;
+        r = i == 3 ? P[3] : r;
+        r = i == 4 ? P[4] : r;
+        r = i == 5 ? P[5] : r;
+        return r;
+    }
+
     // Signs of dot(X - base, cross(V0 - V1, W0 - W1)) for X in x[0..2]; `reject` reproduces
     // ((d0 * d1) > 0) && ((d0 * d2) > 0) (tri_tri_intersect.c:421, 438).
     __device__ __forceinline__ void stage(int V0, int V1, int W0, int W1, int base, const int *x, int *s,
@@ -120,10 +143,10 @@ template <bool FP64> struct TriTri {
     {
         tests += 3;
         if (!FP64) {
-            F3e n = fcross(fdiff(F[V0], F[V1]), fdiff(F[W0], F[W1]));
+            F3e n = fcross(fdiff(fs(V0), fs(V1)), fdiff(fs(W0), fs(W1)));
             int ok = 1;
             for (int k = 0; k < 3; ++k) {
-                s[k] = fdot_sign(fdiff(F[x[k]], F[base]), n);
+                s[k] = fdot_sign(fdiff(fs(x[k]), fs(base)), n);
                 ok &= (s[k] != 0);
             }
             if (ok) {
@@ -133,10 +156,10 @@ template <bool FP64> struct TriTri {
             fallbacks += 3;
             load64();
         }
-        d3 n = cross(P[V0] - P[V1], P[W0] - P[W1]);
+        d3 n = cross(ps(V0) - ps(V1), ps(W0) - ps(W1));
         double d[3];
         for (int k = 0; k < 3; ++k) {
-            d[k] = dot(P[x[k]] - P[base], n);
+            d[k] = dot(ps(x[k]) - ps(base), n);
             s[k] = sign64(d[k]);
         }
         reject = ((d[0] * d[1]) > 0.0) && ((d[0] * d[2]) > 0.0);
@@ -147,25 +170,25 @@ template <bool FP64> struct TriTri {
     {
         ++tests;
         if (!FP64) {
-            F3e n = fcross(fdiff(F[V0], F[V1]), fdiff(F[W0], F[W1]));
-            int s = fdot_sign(fdiff(F[U0], F[U1]), n);
+            F3e n = fcross(fdiff(fs(V0), fs(V1)), fdiff(fs(W0), fs(W1)));
+            int s = fdot_sign(fdiff(fs(U0), fs(U1)), n);
             if (s != 0)
                 return s;
             ++fallbacks;
             load64();
         }
-        d3 n = cross(P[V0] - P[V1], P[W0] - P[W1]);
-        return sign64(dot(P[U0] - P[U1], n));
+        d3 n = cross(ps(V0) - ps(V1), ps(W0) - ps(W1));
+        return sign64(dot(ps(U0) - ps(U1), n));
     }
 
     // out = base - alpha * (base - other), alpha = dot(base - ref, n) / dot(base - other, n)
     __device__ __forceinline__ d3 along(int base, int ref, int other, d3 n)
     {
-        d3 v1 = P[base] - P[ref];
-        d3 v2 = P[base] - P[other];
+        d3 v1 = ps(base) - ps(ref);
+        d3 v2 = ps(base) - ps(other);
         double alpha = dot(v1, n) / dot(v2, n);
         d3 sv = scale(alpha, v2);
-        return P[base] - sv;
+        return ps(base) - sv;
     }
 
     // CONSTRUCT_INTERSECTION (tri_tri_intersect.c:285-356) on slots already in canonical order
@@ -185,8 +208,8 @@ template <bool FP64> struct TriTri {
             which = orient(p2, p1, r1, p1, q2, p1) >= 0 ? 2 : 3;
         }
         load64();
-        d3 N1 = cross(P[1] - P[0], P[2] - P[0]);
-        d3 N2 = cross(P[3] - P[5], P[4] - P[5]);
+        d3 N1 = cross(ps(1) - ps(0), ps(2) - ps(0));
+        d3 N2 = cross(ps(3) - ps(5), ps(4) - ps(5));
         d3 s, t;
         if (which == 0) {
             s = along(p1, p2, r1, N2);

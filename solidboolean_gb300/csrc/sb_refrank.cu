@@ -35,6 +35,14 @@ struct RNode {
     double sum[3], asum[3];          // approximate sum of member centres and of their magnitudes
 };
 
+// one triangle's data, kept physically in the current permutation order so every pass reads it coalesced
+struct RElem {
+    double c[3];   // box centre
+    double bx[6];  // box lo xyz, hi xyz
+    int tri;
+    int pad;
+};
+
 __device__ __forceinline__ void rnode_init(RNode &n, int begin, int count)
 {
     n.begin = begin;
@@ -54,19 +62,24 @@ __device__ __forceinline__ void rnode_init(RNode &n, int begin, int count)
 
 // box centre of each triangle, exactly as AxisAlignedBoudingBox::updateCenter computes it
 // (((0 + v0) + v1) + v2) / (float)3 (src/axisalignedboundingbox.h:31-53)
-__global__ void k_rr_centres(int nt, const double *__restrict__ v, const uint32_t *__restrict__ t, double *cen,
-                             int *perm, int *nodeOf)
+__global__ void k_rr_centres(int nt, const double *__restrict__ v, const uint32_t *__restrict__ t,
+                             const double *__restrict__ box64, RElem *rec, int *nodeOf)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nt)
         return;
+    RElem e;
     for (int a = 0; a < 3; ++a) {
         double s = 0.0;
         for (int k = 0; k < 3; ++k)
             s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
-        cen[3 * (size_t)i + a] = s / 3.0;
+        e.c[a] = s / 3.0;
     }
-    perm[i] = i;
+    for (int k = 0; k < 6; ++k)
+        e.bx[k] = box64[6 * (size_t)i + k];
+    e.tri = i;
+    e.pad = 0;
+    rec[i] = e;
     nodeOf[i] = 0;
 }
 
@@ -165,12 +178,12 @@ __device__ void rr_block_accumulate(RNode *nodes, int node, const double *c, con
     }
 }
 
-__global__ void k_rr_root(int nt, const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
+__global__ void k_rr_root(int nt, const RElem *__restrict__ rec, RNode *nodes)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int node = i < nt ? 0 : -1;
-    int j = i < nt ? i : 0;
-    rr_block_accumulate(nodes, node, cen + 3 * (size_t)j, box64 + 6 * (size_t)j);
+    const RElem &e = rec[i < nt ? i : 0];
+    rr_block_accumulate(nodes, node, e.c, e.bx);
 }
 
 // gamma_n = n u / (1 - n u), rounded up
@@ -213,8 +226,8 @@ __global__ void k_rr_prep(const int *__restrict__ bounds, RNode *nodes, int *cou
 }
 
 // flag: 1 = left, 0 = right; positions of leaves are left untouched (flag 0)
-__global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const int *__restrict__ perm,
-                              const int *__restrict__ nodeOf, const double *__restrict__ cen, RNode *nodes, int *flag)
+__global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const RElem *__restrict__ rec,
+                              const int *__restrict__ nodeOf, RNode *nodes, int *flag)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nt)
@@ -224,7 +237,7 @@ __global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const int 
     if (id >= bounds[0]) {
         RNode &n = nodes[id];
         if (n.count > 20) {
-            double c = cen[3 * (size_t)perm[p] + n.axis];
+            double c = rec[p].c[n.axis];
             if (c < n.clo)
                 f = 1;
             else if (!(c >= n.chi))
@@ -235,8 +248,8 @@ __global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const int 
 }
 
 // nodes whose interval could not decide every member: the reference's sequential sum, in member order
-__global__ void k_rr_resolve(const int *__restrict__ bounds, const int *__restrict__ perm,
-                             const double *__restrict__ cen, RNode *nodes, int *flag)
+__global__ void k_rr_resolve(const int *__restrict__ bounds, const RElem *__restrict__ rec, RNode *nodes,
+                             int *flag)
 {
     const int first = bounds[0], last = bounds[1];
     for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
@@ -245,10 +258,10 @@ __global__ void k_rr_resolve(const int *__restrict__ bounds, const int *__restri
             continue;
         double s = 0.0;
         for (int p = n.begin; p < n.begin + n.count; ++p)
-            s = s + cen[3 * (size_t)perm[p] + n.axis];
+            s = s + rec[p].c[n.axis];
         double split = s / (double)(float)n.count;
         for (int p = n.begin; p < n.begin + n.count; ++p)
-            flag[p] = cen[3 * (size_t)perm[p] + n.axis] < split ? 1 : 0;
+            flag[p] = rec[p].c[n.axis] < split ? 1 : 0;
     }
 }
 
@@ -281,17 +294,22 @@ __global__ void k_rr_children(const int *__restrict__ bounds, const int *__restr
     }
 }
 
-__global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const int *__restrict__ perm,
+// nodeOf: >= 0 node of the current level, -2 settled in a leaf with its record already in both buffers
+__global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const RElem *__restrict__ rec,
                              const int *__restrict__ nodeOf, const int *__restrict__ flag,
-                             const int *__restrict__ scan, const RNode *nodes, int *perm2, int *nodeOf2)
+                             const int *__restrict__ scan, const RNode *nodes, RElem *rec2, int *nodeOf2)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nt)
         return;
     int id = nodeOf[p];
-    if (id < bounds[0] || nodes[id].count <= 20) {
-        perm2[p] = perm[p];
-        nodeOf2[p] = -1; // settled in a leaf
+    if (id == -2) {
+        nodeOf2[p] = -2;
+        return;
+    }
+    if (id < 0 || id < bounds[0] || nodes[id].count <= 20) {
+        rec2[p] = rec[p]; // settled in a leaf: one copy makes it final in both buffers
+        nodeOf2[p] = -2;
         return;
     }
     const RNode &n = nodes[id];
@@ -306,17 +324,17 @@ __global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const int *
     else
         pos = flag[p] ? (left - 1 - lrank) : (left + rrank);
     int q = n.begin + pos;
-    perm2[q] = perm[p];
+    rec2[q] = rec[p];
     nodeOf2[q] = pos < n.leftFinal ? n.child : n.child + 1;
 }
 
-__global__ void k_rr_child_stats(int nt, const int *__restrict__ perm, const int *__restrict__ nodeOf,
-                                 const double *__restrict__ cen, const double *__restrict__ box64, RNode *nodes)
+__global__ void k_rr_child_stats(int nt, const RElem *__restrict__ rec, const int *__restrict__ nodeOf,
+                                 RNode *nodes)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int id = p < nt ? nodeOf[p] : -1;
-    int t = id >= 0 ? perm[p] : 0;
-    rr_block_accumulate(nodes, id, cen + 3 * (size_t)t, box64 + 6 * (size_t)t);
+    const RElem &e = rec[id >= 0 ? p : 0];
+    rr_block_accumulate(nodes, id < 0 ? -1 : id, e.c, e.bx);
 }
 
 // next level: [last, nodes allocated so far)
@@ -326,11 +344,11 @@ __global__ void k_rr_advance(int *bounds, const int *counters)
     bounds[1] = counters[0];
 }
 
-__global__ void k_rr_rank(int nt, const int *__restrict__ perm, int *rank)
+__global__ void k_rr_rank(int nt, const RElem *__restrict__ rec, int *rank)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < nt)
-        rank[perm[p]] = p;
+        rank[rec[p].tri] = p;
 }
 
 __global__ void k_rr_init_root(RNode *nodes, int nt, int *counters)
@@ -355,22 +373,21 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int *)nullptr, (int *)nullptr, nt + 1, s);
     Carve c;
-    size_t o_cen = c.take<double>(3 * (size_t)nt);
-    size_t o_p1 = c.take<int>(nt), o_p2 = c.take<int>(nt), o_n1 = c.take<int>(nt), o_n2 = c.take<int>(nt);
+    size_t o_r1 = c.take<RElem>(nt), o_r2 = c.take<RElem>(nt), o_n1 = c.take<int>(nt), o_n2 = c.take<int>(nt);
     size_t o_fl = c.take<int>(nt + 1), o_sc = c.take<int>(nt + 1);
     size_t o_nd = c.take<RNode>(maxNodes), o_ct = c.take<int>(8), o_cub = c.take<char>(scanBytes);
     SB_CUDA_CHECK(m->tmp.ensure(c.off));
     char *b = m->tmp.as<char>();
-    double *cen = (double *)(b + o_cen);
-    int *perm = (int *)(b + o_p1), *perm2 = (int *)(b + o_p2), *nodeOf = (int *)(b + o_n1), *nodeOf2 = (int *)(b + o_n2);
+    RElem *rec = (RElem *)(b + o_r1), *rec2 = (RElem *)(b + o_r2);
+    int *nodeOf = (int *)(b + o_n1), *nodeOf2 = (int *)(b + o_n2);
     int *flag = (int *)(b + o_fl), *scan = (int *)(b + o_sc);
     RNode *nodes = (RNode *)(b + o_nd);
     int *counters = (int *)(b + o_ct); // [0] nodes, [1] leaves, [3] overflow, [4..5] level bounds
     int *bounds = counters + 4;
     const int BS = 256, G = (nt + BS - 1) / BS, GN = 152 * 4;
-    SB_COUNT(k_rr_centres)<<<G, BS, 0, s>>>(nt, d.v, d.t, cen, perm, nodeOf);
+    SB_COUNT(k_rr_centres)<<<G, BS, 0, s>>>(nt, d.v, d.t, d.box64, rec, nodeOf);
     SB_COUNT(k_rr_init_root)<<<1, 1, 0, s>>>(nodes, nt, counters);
-    SB_COUNT(k_rr_root)<<<G, BS, 0, s>>>(nt, cen, d.box64, nodes);
+    SB_COUNT(k_rr_root)<<<G, BS, 0, s>>>(nt, rec, nodes);
     SB_CUDA_CHECK(cudaMemsetAsync(flag + nt, 0, sizeof(int), s));
     // levels run in batches; the host looks at the level bounds only between batches
     const int kBatch = 6;
@@ -378,14 +395,14 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     for (int level = 0; level < 4096 && !done; level += kBatch) {
         for (int j = 0; j < kBatch; ++j) {
             SB_COUNT(k_rr_prep)<<<GN, 128, 0, s>>>(bounds, nodes, counters);
-            SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, bounds, perm, nodeOf, cen, nodes, flag);
-            SB_COUNT(k_rr_resolve)<<<GN, 128, 0, s>>>(bounds, perm, cen, nodes, flag);
+            SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, bounds, rec, nodeOf, nodes, flag);
+            SB_COUNT(k_rr_resolve)<<<GN, 128, 0, s>>>(bounds, rec, nodes, flag);
             SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
             SB_COUNT(k_rr_children)<<<GN, 128, 0, s>>>(bounds, scan, nodes, counters, maxNodes);
-            SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, bounds, perm, nodeOf, flag, scan, nodes, perm2, nodeOf2);
-            SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, perm2, nodeOf2, cen, d.box64, nodes);
+            SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, bounds, rec, nodeOf, flag, scan, nodes, rec2, nodeOf2);
+            SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, rec2, nodeOf2, nodes);
             SB_COUNT(k_rr_advance)<<<1, 1, 0, s>>>(bounds, counters);
-            std::swap(perm, perm2);
+            std::swap(rec, rec2);
             std::swap(nodeOf, nodeOf2);
         }
         int cnt[8];
@@ -401,7 +418,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
         set_last_error("reference tree deeper than 4096 levels");
         return SB_ERR_CAPACITY;
     }
-    SB_COUNT(k_rr_rank)<<<G, BS, 0, s>>>(nt, perm, d.rank);
+    SB_COUNT(k_rr_rank)<<<G, BS, 0, s>>>(nt, rec, d.rank);
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = true;
     return SB_OK;
