@@ -26,6 +26,11 @@
 
 namespace sbg {
 
+// nodes with at most kSub members are finished by one block each (k_rr_subtree)
+constexpr int kSub = 2048;
+constexpr int kSubThreads = 256;
+constexpr int kSubNodes = 512;
+
 struct RNode {
     int begin, count;
     int axis, leftFinal, child; // child: id of the left child (right = child + 1), -1 for a leaf
@@ -195,14 +200,17 @@ __device__ __forceinline__ double rr_gamma(int n)
 }
 
 // bounds[0..1]: first and one-past-last node of the current level; counters[1] counts leaves
-__global__ void k_rr_prep(const int *__restrict__ bounds, RNode *nodes, int *counters)
+__global__ void k_rr_prep(const int *__restrict__ bounds, RNode *nodes, int *counters, int *deferred)
 {
     const int first = bounds[0], last = bounds[1];
     for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
         RNode &n = nodes[id];
-        if (n.count <= 20) {
+        if (n.count <= kSub) {
             n.child = -1;
-            atomicAdd(counters + 1, 1);
+            if (n.count <= 20)
+                atomicAdd(counters + 1, 1);
+            else
+                deferred[atomicAdd(counters + 6, 1)] = id;
             continue;
         }
         float span[3];
@@ -236,7 +244,7 @@ __global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const REle
     int f = 0;
     if (id >= bounds[0]) {
         RNode &n = nodes[id];
-        if (n.count > 20) {
+        if (n.count > kSub) {
             double c = rec[p].c[n.axis];
             if (c < n.clo)
                 f = 1;
@@ -254,7 +262,7 @@ __global__ void k_rr_resolve(const int *__restrict__ bounds, const RElem *__rest
     const int first = bounds[0], last = bounds[1];
     for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
         RNode &n = nodes[id];
-        if (n.count <= 20 || !n.ambiguous)
+        if (n.count <= kSub || !n.ambiguous)
             continue;
         double s = 0.0;
         for (int p = n.begin; p < n.begin + n.count; ++p)
@@ -271,7 +279,7 @@ __global__ void k_rr_children(const int *__restrict__ bounds, const int *__restr
     const int first = bounds[0], last = bounds[1];
     for (int id = first + blockIdx.x * blockDim.x + threadIdx.x; id < last; id += gridDim.x * blockDim.x) {
         RNode &n = nodes[id];
-        if (n.count <= 20)
+        if (n.count <= kSub)
             continue;
         int left = scan[n.begin + n.count] - scan[n.begin];
         int right = n.count - left;
@@ -307,7 +315,7 @@ __global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const RElem
         nodeOf2[p] = -2;
         return;
     }
-    if (id < 0 || id < bounds[0] || nodes[id].count <= 20) {
+    if (id < 0 || id < bounds[0] || nodes[id].count <= kSub) {
         rec2[p] = rec[p]; // settled in a leaf: one copy makes it final in both buffers
         nodeOf2[p] = -2;
         return;
@@ -337,6 +345,277 @@ __global__ void k_rr_child_stats(int nt, const RElem *__restrict__ rec, const in
     rr_block_accumulate(nodes, id < 0 ? -1 : id, e.c, e.bx);
 }
 
+
+// ---------------------------------------------------------------------------------------------------
+// One block finishes the subtree of one node with at most kSub members: the same level loop as above,
+// with the node records and per-element state in shared memory and __syncthreads between the steps.
+// ---------------------------------------------------------------------------------------------------
+struct SNode {
+    int begin, count, axis, leftFinal, child, ambiguous;
+    double clo, chi;
+    unsigned long long lo[3], hi[3];
+    double sum[3], asum[3];
+};
+
+__device__ __forceinline__ void snode_init(SNode &n, int begin, int count)
+{
+    n.begin = begin;
+    n.count = count;
+    n.axis = 0;
+    n.leftFinal = 0;
+    n.child = -1;
+    n.ambiguous = 0;
+    n.clo = n.chi = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        n.lo[k] = ~0ull;
+        n.hi[k] = 0ull;
+        n.sum[k] = 0.0;
+        n.asum[k] = 0.0;
+    }
+}
+
+// warp-reduced accumulation into a shared-memory node (lanes of one node combine first)
+__device__ __forceinline__ void snode_accumulate(SNode *nodes, int node, const RElem &e, bool valid)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    int key = valid ? node : -1;
+    int lead = __shfl_sync(full, key, 0);
+    bool uniform = __all_sync(full, key == lead) && lead >= 0;
+    unsigned long long lo[3], hi[3];
+    double sm[3], as[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = valid ? dbl_to_ord(e.bx[k]) : ~0ull;
+        hi[k] = valid ? dbl_to_ord(e.bx[3 + k]) : 0ull;
+        sm[k] = valid ? e.c[k] : 0.0;
+        as[k] = valid ? fabs(e.c[k]) : 0.0;
+    }
+    if (uniform) {
+        for (int o = 16; o > 0; o >>= 1)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = min(lo[k], __shfl_xor_sync(full, lo[k], o));
+                hi[k] = max(hi[k], __shfl_xor_sync(full, hi[k], o));
+                sm[k] += __shfl_xor_sync(full, sm[k], o);
+                as[k] += __shfl_xor_sync(full, as[k], o);
+            }
+        if ((threadIdx.x & 31) != 0)
+            return;
+    } else if (!valid) {
+        return;
+    }
+    SNode &n = nodes[node];
+    for (int k = 0; k < 3; ++k) {
+        atomicMin(&n.lo[k], lo[k]);
+        atomicMax(&n.hi[k], hi[k]);
+        atomicAdd(&n.sum[k], sm[k]);
+        atomicAdd(&n.asum[k], as[k]);
+    }
+}
+
+__global__ void __launch_bounds__(kSubThreads)
+    k_rr_subtree(const int *__restrict__ deferred, const RNode *__restrict__ gnodes, RElem *recA, RElem *recB,
+                 int *rank, int *errors)
+{
+    // ~102 KB of dynamic shared memory (opted in by the host)
+    extern __shared__ __align__(16) unsigned char smem[];
+    SNode *nodes = reinterpret_cast<SNode *>(smem);
+    int(*nodeOf)[kSub] = reinterpret_cast<int(*)[kSub]>(smem + sizeof(SNode) * kSubNodes);
+    int *flag = reinterpret_cast<int *>(smem + sizeof(SNode) * kSubNodes + sizeof(int) * 2 * kSub);
+    int *scan = flag + kSub;
+    int *warpSum = scan + kSub + 1;
+    __shared__ int nNodes, lFirst, lLast, anyAmb, err;
+    const int tid = threadIdx.x;
+    const RNode &g = gnodes[deferred[blockIdx.x]];
+    const int base = g.begin, n = g.count;
+    RElem *buf[2] = {recA + base, recB + base};
+    if (tid == 0) {
+        SNode &r = nodes[0];
+        r.begin = 0;
+        r.count = n;
+        r.axis = 0;
+        r.leftFinal = 0;
+        r.child = -1;
+        r.ambiguous = 0;
+        for (int k = 0; k < 3; ++k) {
+            r.lo[k] = g.lo[k];
+            r.hi[k] = g.hi[k];
+            r.sum[k] = g.sum[k];
+            r.asum[k] = g.asum[k];
+        }
+        nNodes = 1;
+        lFirst = 0;
+        lLast = 1;
+        err = 0;
+    }
+    for (int p = tid; p < n; p += kSubThreads)
+        nodeOf[0][p] = 0;
+    __syncthreads();
+    int cur = 0;
+    for (int level = 0; level < 4 * kSub; ++level) {
+        const int first = lFirst, last = lLast;
+        if (first >= last || err)
+            break;
+        // prep
+        for (int id = first + tid; id < last; id += kSubThreads) {
+            SNode &nd = nodes[id];
+            if (nd.count <= 20) {
+                nd.child = -1;
+                continue;
+            }
+            float span[3];
+            for (int k = 0; k < 3; ++k)
+                span[k] = __double2float_rn(ord_to_dbl(nd.hi[k]) - ord_to_dbl(nd.lo[k]));
+            int axis = 0;
+            for (int k = 1; k < 3; ++k)
+                if (span[axis] < span[k])
+                    axis = k;
+            nd.axis = axis;
+            double gm = rr_gamma(nd.count + 1);
+            double aup = __dmul_ru(nd.asum[axis], __dadd_ru(1.0, __dmul_ru(2.0, gm)));
+            double e = __dadd_ru(__dmul_ru(__dmul_ru(2.0, gm), aup), 1e-300);
+            double cnt = (double)(float)nd.count;
+            nd.clo = __ddiv_rd(__dsub_rd(nd.sum[axis], e), cnt);
+            nd.chi = __ddiv_ru(__dadd_ru(nd.sum[axis], e), cnt);
+            nd.ambiguous = 0;
+        }
+        if (tid == 0)
+            anyAmb = 0;
+        __syncthreads();
+        // classify
+        const RElem *rc = buf[cur];
+        for (int p = tid; p < n; p += kSubThreads) {
+            int id = nodeOf[cur][p];
+            int f = 0;
+            if (id >= first) {
+                SNode &nd = nodes[id];
+                if (nd.count > 20) {
+                    double c = rc[p].c[nd.axis];
+                    if (c < nd.clo)
+                        f = 1;
+                    else if (!(c >= nd.chi)) {
+                        nd.ambiguous = 1;
+                        anyAmb = 1;
+                    }
+                }
+            }
+            flag[p] = f;
+        }
+        __syncthreads();
+        if (anyAmb) {
+            for (int id = first + tid; id < last; id += kSubThreads) {
+                SNode &nd = nodes[id];
+                if (nd.count <= 20 || !nd.ambiguous)
+                    continue;
+                double sacc = 0.0;
+                for (int p = nd.begin; p < nd.begin + nd.count; ++p)
+                    sacc = sacc + rc[p].c[nd.axis];
+                double split = sacc / (double)(float)nd.count;
+                for (int p = nd.begin; p < nd.begin + nd.count; ++p)
+                    flag[p] = rc[p].c[nd.axis] < split ? 1 : 0;
+            }
+            __syncthreads();
+        }
+        // block exclusive scan of flag[0..n): each thread owns a contiguous run of kSub / kSubThreads slots
+        {
+            const int per = kSub / kSubThreads;
+            const int b0 = tid * per;
+            int local = 0;
+            for (int j = 0; j < per; ++j)
+                local += (b0 + j < n) ? flag[b0 + j] : 0;
+            int incl = local;
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if ((tid & 31) >= o)
+                    incl += v;
+            }
+            if ((tid & 31) == 31)
+                warpSum[tid >> 5] = incl;
+            __syncthreads();
+            int woff = 0;
+            for (int w = 0; w < (tid >> 5); ++w)
+                woff += warpSum[w];
+            int run = woff + incl - local;
+            for (int j = 0; j < per; ++j) {
+                if (b0 + j <= n)
+                    scan[b0 + j] = run;
+                run += (b0 + j < n) ? flag[b0 + j] : 0;
+            }
+            if (tid == kSubThreads - 1)
+                scan[n] = run;
+        }
+        __syncthreads();
+        // children
+        for (int id = first + tid; id < last; id += kSubThreads) {
+            SNode &nd = nodes[id];
+            if (nd.count <= 20)
+                continue;
+            int left = scan[nd.begin + nd.count] - scan[nd.begin];
+            int right = nd.count - left;
+            int lf = left;
+            if (left == 0)
+                lf = right / 2;
+            else if (right == 0)
+                lf = left - left / 2;
+            int c = atomicAdd(&nNodes, 2);
+            if (c + 2 > kSubNodes) {
+                err = 1;
+                nd.count = 0;
+                continue;
+            }
+            nd.leftFinal = lf;
+            nd.child = c;
+            snode_init(nodes[c], nd.begin, lf);
+            snode_init(nodes[c + 1], nd.begin + lf, nd.count - lf);
+        }
+        __syncthreads();
+        // scatter into the other buffer
+        RElem *dst = buf[cur ^ 1];
+        for (int p = tid; p < n; p += kSubThreads) {
+            int id = nodeOf[cur][p];
+            if (id < first || nodes[id].count <= 20) {
+                dst[p] = rc[p];
+                nodeOf[cur ^ 1][p] = -1;
+                continue;
+            }
+            const SNode &nd = nodes[id];
+            int left = scan[nd.begin + nd.count] - scan[nd.begin];
+            int lrank = scan[p] - scan[nd.begin];
+            int rrank = (p - nd.begin) - lrank;
+            int pos;
+            if (left == 0)
+                pos = rrank;
+            else if (left == nd.count)
+                pos = nd.count - 1 - lrank;
+            else
+                pos = flag[p] ? (left - 1 - lrank) : (left + rrank);
+            int q = nd.begin + pos;
+            dst[q] = rc[p];
+            nodeOf[cur ^ 1][q] = pos < nd.leftFinal ? nd.child : nd.child + 1;
+        }
+        __syncthreads();
+        // statistics of the new nodes, read back in the new order
+        for (int p0 = 0; p0 < n; p0 += kSubThreads) {
+            int p = p0 + tid;
+            bool valid = p < n && nodeOf[cur ^ 1][p] >= 0;
+            RElem e;
+            if (valid)
+                e = dst[p];
+            snode_accumulate(nodes, valid ? nodeOf[cur ^ 1][p] : 0, e, valid);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            lFirst = last;
+            lLast = nNodes;
+        }
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (tid == 0 && (err || lFirst < lLast))
+        atomicAdd(errors, 1);
+    const RElem *fin = buf[cur];
+    for (int p = tid; p < n; p += kSubThreads)
+        rank[fin[p].tri] = base + p;
+}
+
 // next level: [last, nodes allocated so far)
 __global__ void k_rr_advance(int *bounds, const int *counters)
 {
@@ -359,6 +638,8 @@ __global__ void k_rr_init_root(RNode *nodes, int nt, int *counters)
     counters[3] = 0; // capacity overflow
     counters[4] = 0; // level bounds: first
     counters[5] = 1; //               one past last
+    counters[6] = 0; // deferred subtrees
+    counters[7] = 0; // subtree errors
 }
 
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
@@ -376,6 +657,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     size_t o_r1 = c.take<RElem>(nt), o_r2 = c.take<RElem>(nt), o_n1 = c.take<int>(nt), o_n2 = c.take<int>(nt);
     size_t o_fl = c.take<int>(nt + 1), o_sc = c.take<int>(nt + 1);
     size_t o_nd = c.take<RNode>(maxNodes), o_ct = c.take<int>(8), o_cub = c.take<char>(scanBytes);
+    size_t o_df = c.take<int>(maxNodes);
     SB_CUDA_CHECK(m->tmp.ensure(c.off));
     char *b = m->tmp.as<char>();
     RElem *rec = (RElem *)(b + o_r1), *rec2 = (RElem *)(b + o_r2);
@@ -384,6 +666,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     RNode *nodes = (RNode *)(b + o_nd);
     int *counters = (int *)(b + o_ct); // [0] nodes, [1] leaves, [3] overflow, [4..5] level bounds
     int *bounds = counters + 4;
+    int *deferred = (int *)(b + o_df);
     const int BS = 256, G = (nt + BS - 1) / BS, GN = 152 * 4;
     SB_COUNT(k_rr_centres)<<<G, BS, 0, s>>>(nt, d.v, d.t, d.box64, rec, nodeOf);
     SB_COUNT(k_rr_init_root)<<<1, 1, 0, s>>>(nodes, nt, counters);
@@ -394,7 +677,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     bool done = false;
     for (int level = 0; level < 4096 && !done; level += kBatch) {
         for (int j = 0; j < kBatch; ++j) {
-            SB_COUNT(k_rr_prep)<<<GN, 128, 0, s>>>(bounds, nodes, counters);
+            SB_COUNT(k_rr_prep)<<<GN, 128, 0, s>>>(bounds, nodes, counters, deferred);
             SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, bounds, rec, nodeOf, nodes, flag);
             SB_COUNT(k_rr_resolve)<<<GN, 128, 0, s>>>(bounds, rec, nodes, flag);
             SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
@@ -419,6 +702,22 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
         return SB_ERR_CAPACITY;
     }
     SB_COUNT(k_rr_rank)<<<G, BS, 0, s>>>(nt, rec, d.rank);
+    int cnt2[8];
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnt2, counters, sizeof cnt2, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (cnt2[6] > 0) {
+        const size_t smemBytes = sizeof(SNode) * kSubNodes + sizeof(int) * (2 * kSub + kSub + kSub + 1 + kSubThreads / 32);
+        SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes));
+        SB_COUNT(k_rr_subtree)<<<cnt2[6], kSubThreads, smemBytes, s>>>(deferred, nodes, rec, rec2, d.rank,
+                                                                       counters + 7);
+        int errs = 0;
+        SB_CUDA_CHECK(cudaMemcpyAsync(&errs, counters + 7, sizeof errs, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        if (errs) {
+            set_last_error("reference tree: a subtree exceeded its node records");
+            return SB_ERR_CAPACITY;
+        }
+    }
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = true;
     return SB_OK;
