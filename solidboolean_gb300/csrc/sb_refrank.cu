@@ -238,7 +238,7 @@ __global__ void k_rr_classify(int nt, const int *__restrict__ bounds, const REle
                               const int *__restrict__ nodeOf, RNode *nodes, int *flag)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nt)
+    if (p >= nt || bounds[0] >= bounds[1])
         return;
     int id = nodeOf[p];
     int f = 0;
@@ -308,7 +308,7 @@ __global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const RElem
                              const int *__restrict__ scan, const RNode *nodes, RElem *rec2, int *nodeOf2)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nt)
+    if (p >= nt || bounds[0] >= bounds[1])
         return;
     int id = nodeOf[p];
     if (id == -2) {
@@ -336,9 +336,12 @@ __global__ void k_rr_scatter(int nt, const int *__restrict__ bounds, const RElem
     nodeOf2[q] = pos < n.leftFinal ? n.child : n.child + 1;
 }
 
-__global__ void k_rr_child_stats(int nt, const RElem *__restrict__ rec, const int *__restrict__ nodeOf,
-                                 RNode *nodes)
+__global__ void k_rr_child_stats(int nt, const int *__restrict__ bounds, const RElem *__restrict__ rec,
+                                 const int *__restrict__ nodeOf, RNode *nodes)
 {
+    // an empty level wrote no indices: the other buffer still holds an older level's (block-uniform exit)
+    if (bounds[0] >= bounds[1])
+        return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int id = p < nt ? nodeOf[p] : -1;
     const RElem &e = rec[id >= 0 ? p : 0];
@@ -419,14 +422,16 @@ __global__ void __launch_bounds__(kSubThreads)
     extern __shared__ __align__(16) unsigned char smem[];
     SNode *nodes = reinterpret_cast<SNode *>(smem);
     int(*nodeOf)[kSub] = reinterpret_cast<int(*)[kSub]>(smem + sizeof(SNode) * kSubNodes);
-    int *flag = reinterpret_cast<int *>(smem + sizeof(SNode) * kSubNodes + sizeof(int) * 2 * kSub);
+    int(*perm)[kSub] = reinterpret_cast<int(*)[kSub]>(smem + sizeof(SNode) * kSubNodes + sizeof(int) * 2 * kSub);
+    int *flag = reinterpret_cast<int *>(smem + sizeof(SNode) * kSubNodes + sizeof(int) * 4 * kSub);
     int *scan = flag + kSub;
     int *warpSum = scan + kSub + 1;
     __shared__ int nNodes, lFirst, lLast, anyAmb, err;
     const int tid = threadIdx.x;
     const RNode &g = gnodes[deferred[blockIdx.x]];
     const int base = g.begin, n = g.count;
-    RElem *buf[2] = {recA + base, recB + base};
+    const RElem *rc = recA + base; // the segment's records stay in place; only indices move
+    (void)recB;
     if (tid == 0) {
         SNode &r = nodes[0];
         r.begin = 0;
@@ -446,8 +451,10 @@ __global__ void __launch_bounds__(kSubThreads)
         lLast = 1;
         err = 0;
     }
-    for (int p = tid; p < n; p += kSubThreads)
+    for (int p = tid; p < n; p += kSubThreads) {
         nodeOf[0][p] = 0;
+        perm[0][p] = p;
+    }
     __syncthreads();
     int cur = 0;
     for (int level = 0; level < 4 * kSub; ++level) {
@@ -481,14 +488,13 @@ __global__ void __launch_bounds__(kSubThreads)
             anyAmb = 0;
         __syncthreads();
         // classify
-        const RElem *rc = buf[cur];
         for (int p = tid; p < n; p += kSubThreads) {
             int id = nodeOf[cur][p];
             int f = 0;
             if (id >= first) {
                 SNode &nd = nodes[id];
                 if (nd.count > 20) {
-                    double c = rc[p].c[nd.axis];
+                    double c = rc[perm[cur][p]].c[nd.axis];
                     if (c < nd.clo)
                         f = 1;
                     else if (!(c >= nd.chi)) {
@@ -507,10 +513,10 @@ __global__ void __launch_bounds__(kSubThreads)
                     continue;
                 double sacc = 0.0;
                 for (int p = nd.begin; p < nd.begin + nd.count; ++p)
-                    sacc = sacc + rc[p].c[nd.axis];
+                    sacc = sacc + rc[perm[cur][p]].c[nd.axis];
                 double split = sacc / (double)(float)nd.count;
                 for (int p = nd.begin; p < nd.begin + nd.count; ++p)
-                    flag[p] = rc[p].c[nd.axis] < split ? 1 : 0;
+                    flag[p] = rc[perm[cur][p]].c[nd.axis] < split ? 1 : 0;
             }
             __syncthreads();
         }
@@ -567,12 +573,11 @@ __global__ void __launch_bounds__(kSubThreads)
             snode_init(nodes[c + 1], nd.begin + lf, nd.count - lf);
         }
         __syncthreads();
-        // scatter into the other buffer
-        RElem *dst = buf[cur ^ 1];
+        // scatter the indices into the other buffer
         for (int p = tid; p < n; p += kSubThreads) {
             int id = nodeOf[cur][p];
             if (id < first || nodes[id].count <= 20) {
-                dst[p] = rc[p];
+                perm[cur ^ 1][p] = perm[cur][p];
                 nodeOf[cur ^ 1][p] = -1;
                 continue;
             }
@@ -588,7 +593,7 @@ __global__ void __launch_bounds__(kSubThreads)
             else
                 pos = flag[p] ? (left - 1 - lrank) : (left + rrank);
             int q = nd.begin + pos;
-            dst[q] = rc[p];
+            perm[cur ^ 1][q] = perm[cur][p];
             nodeOf[cur ^ 1][q] = pos < nd.leftFinal ? nd.child : nd.child + 1;
         }
         __syncthreads();
@@ -598,7 +603,7 @@ __global__ void __launch_bounds__(kSubThreads)
             bool valid = p < n && nodeOf[cur ^ 1][p] >= 0;
             RElem e;
             if (valid)
-                e = dst[p];
+                e = rc[perm[cur ^ 1][p]];
             snode_accumulate(nodes, valid ? nodeOf[cur ^ 1][p] : 0, e, valid);
         }
         __syncthreads();
@@ -611,9 +616,8 @@ __global__ void __launch_bounds__(kSubThreads)
     }
     if (tid == 0 && (err || lFirst < lLast))
         atomicAdd(errors, 1);
-    const RElem *fin = buf[cur];
     for (int p = tid; p < n; p += kSubThreads)
-        rank[fin[p].tri] = base + p;
+        rank[rc[perm[cur][p]].tri] = base + p;
 }
 
 // next level: [last, nodes allocated so far)
@@ -673,17 +677,21 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     SB_COUNT(k_rr_root)<<<G, BS, 0, s>>>(nt, rec, nodes);
     SB_CUDA_CHECK(cudaMemsetAsync(flag + nt, 0, sizeof(int), s));
     // levels run in batches; the host looks at the level bounds only between batches
-    const int kBatch = 6;
+    // the first batch covers the expected depth of the large-node phase (a mean split roughly halves),
+    // later batches are short; empty levels cost only their launches
+    int expected = 1;
+    while ((nt >> expected) > kSub)
+        ++expected;
     bool done = false;
-    for (int level = 0; level < 4096 && !done; level += kBatch) {
-        for (int j = 0; j < kBatch; ++j) {
+    for (int level = 0, batch = expected + 1; level < 4096 && !done; level += batch, batch = 2) {
+        for (int j = 0; j < batch; ++j) {
             SB_COUNT(k_rr_prep)<<<GN, 128, 0, s>>>(bounds, nodes, counters, deferred);
             SB_COUNT(k_rr_classify)<<<G, BS, 0, s>>>(nt, bounds, rec, nodeOf, nodes, flag);
             SB_COUNT(k_rr_resolve)<<<GN, 128, 0, s>>>(bounds, rec, nodes, flag);
             SB_CUDA_CHECK(cub::DeviceScan::ExclusiveSum(b + o_cub, scanBytes, flag, scan, nt + 1, s));
             SB_COUNT(k_rr_children)<<<GN, 128, 0, s>>>(bounds, scan, nodes, counters, maxNodes);
             SB_COUNT(k_rr_scatter)<<<G, BS, 0, s>>>(nt, bounds, rec, nodeOf, flag, scan, nodes, rec2, nodeOf2);
-            SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, rec2, nodeOf2, nodes);
+            SB_COUNT(k_rr_child_stats)<<<G, BS, 0, s>>>(nt, bounds, rec2, nodeOf2, nodes);
             SB_COUNT(k_rr_advance)<<<1, 1, 0, s>>>(bounds, counters);
             std::swap(rec, rec2);
             std::swap(nodeOf, nodeOf2);
@@ -706,7 +714,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     SB_CUDA_CHECK(cudaMemcpyAsync(cnt2, counters, sizeof cnt2, cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
     if (cnt2[6] > 0) {
-        const size_t smemBytes = sizeof(SNode) * kSubNodes + sizeof(int) * (2 * kSub + kSub + kSub + 1 + kSubThreads / 32);
+        const size_t smemBytes = sizeof(SNode) * kSubNodes + sizeof(int) * (4 * kSub + kSub + kSub + 1 + kSubThreads / 32);
         SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes));
         SB_COUNT(k_rr_subtree)<<<cnt2[6], kSubThreads, smemBytes, s>>>(deferred, nodes, rec, rec2, d.rank,
                                                                        counters + 7);
