@@ -6,6 +6,7 @@
 // reference compiled without FMA.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -181,6 +182,47 @@ __host__ __device__ inline void hash_iteration_order(const uint64_t *keys, int n
     int k = 0;
     for (int p = head; p >= 0; p = next[p])
         order[k++] = p;
+}
+
+SB_HD uint64_t dbl_bits(double x)
+{
+    uint64_t u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+}
+SB_HD double bits_dbl(uint64_t u)
+{
+    double x;
+    memcpy(&x, &u, sizeof x);
+    return x;
+}
+
+// x / 3 rounded to nearest (ties to even), in integer arithmetic. With x = m 2^e (m the 53-bit significand),
+// N = m 2^11 lies in [2^63, 2^64); q = N / 3 and r = N mod 3 give the exact quotient q + r/3, which has 62
+// or 63 bits; keeping 53 of them and rounding on the dropped bits plus the sticky remainder is the IEEE
+// result. Inputs whose quotient would leave the normal range, infinities and NaNs use the hardware divide.
+SB_HD double div3_rn(double x)
+{
+    const uint64_t u = dbl_bits(x);
+    const int E = (int)((u >> 52) & 0x7FF);
+    if (E < 3 || E == 0x7FF) {
+        if ((u << 1) == 0)
+            return x; // +-0
+        return x / 3.0;
+    }
+    const uint64_t N = ((u & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11;
+    const uint64_t q = N / 3, r = N - 3 * q;
+    const int sh = (q >> 62) ? 10 : 9;
+    uint64_t mant = q >> sh;
+    const uint64_t rem = q & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (r != 0 || (mant & 1))))
+        ++mant;
+    int Er = E - 11 + sh;
+    if (mant >> 53) {
+        mant >>= 1;
+        ++Er;
+    }
+    return bits_dbl((u & 0x8000000000000000ull) | ((uint64_t)Er << 52) | (mant & 0xFFFFFFFFFFFFFull));
 }
 
 #ifdef __CUDACC__

@@ -26,8 +26,9 @@
 //    remains, which matters on a part whose FP64 rate is a small fraction of its integer rate.
 //
 // Phases: nodes with more than kSub members split level by level over all triangles (classify, rare exact
-// resolution, children); one radix sort then lists each remaining node's members in order, and one block per
-// such node finishes its subtree in shared memory and writes the final positions.
+// resolution, children), visiting the triangles in the LBVH's Morton order so that a node's members form
+// long runs for the reductions; one radix sort then lists each remaining node's members in order, and one
+// block per such node finishes its subtree in shared memory and writes the final positions.
 #include <cub/cub.cuh>
 
 #include "sb_common.cuh"
@@ -47,14 +48,13 @@ enum {
     kCtNodes = 0,   // node records allocated
     kCtTerms = 1,   // terminal nodes listed
     kCtOverflow = 2,
-    kCtPool = 3,    // member-list pool use of the current level (exact resolution)
     kCtFirst = 4,   // current level: first node
     kCtLast = 5,    //                one past the last node
     kCtSubErr = 6,  // subtree blocks that ran out of node records
     kCtCount = 8
 };
 
-// one triangle: its box centre and box, in triangle index order
+// one triangle: its box centre and box (stored by Morton position)
 struct RRec {
     double c[3];
     double lo[3], hi[3];
@@ -69,14 +69,24 @@ struct RStat {
 
 struct RNode {
     int begin, count;  // begin: position of the node's first member in the final leaf order
-    int child;         // left child id (right = child + 1), -1 while unsplit or terminal
     int dir;           // member order: 0 ascending triangle index, 1 descending
-    int axis, flags;   // flags bit 0: a member fell inside the interval
-    int mode, pad;     // 0 regular split, 1 left side was empty, 2 right side was empty
-    unsigned long long clo, chi; // order-preserving keys of an interval holding the reference's split value
-    RStat st;                    // the node's own members
-    RStat acc[2];                // left / right members, accumulated while classifying
+    int flags;         // bit 0: a member fell inside the interval
+    int mode, pad[3];  // 0 regular split, 1 left side was empty, 2 right side was empty
+    RStat st;          // the node's own members
+    RStat acc[2];      // left / right members, accumulated while classifying
 };
+
+// what the per-member passes read of a node, in one 32-byte sector
+struct NParam {
+    int child;         // left child id (right = child + 1), -1 while unsplit or terminal
+    int count, axis, pad;
+    unsigned long long clo, chi; // order-preserving keys of an interval holding the reference's split value
+};
+
+// per-member state word: node id << 2 | tag, tag 0 settled in that node, 1 / 2 pending move to its left /
+// right child, 3 inside the node's interval (rewritten by the exact resolution)
+__device__ __forceinline__ int st_node(int v) { return v >> 2; }
+__device__ __forceinline__ int st_tag(int v) { return v & 3; }
 
 // order-preserving key of a double with -0 folded onto +0 (they compare equal)
 __device__ __forceinline__ unsigned long long ordc(double d)
@@ -190,8 +200,9 @@ __device__ __forceinline__ void estat_merge(EStat &a, const EStat &b)
     }
 }
 
-// Segmented inclusive reduction over runs of equal `key` among the 32 lanes. Returns true on the last lane
-// of each run, which then holds the run's total and its length in `len`. All 32 lanes must call it.
+// Segmented inclusive reduction over runs of equal `key` among the 32 lanes; `len` is an int payload summed
+// alongside (1 per member on entry). Returns true on the last lane of each run, which then holds the run's
+// total. All 32 lanes must call it.
 __device__ __forceinline__ bool warp_segment_reduce(int key, EStat &r, int &len)
 {
     const unsigned full = 0xFFFFFFFFu;
@@ -210,29 +221,148 @@ __device__ __forceinline__ bool warp_segment_reduce(int key, EStat &r, int &len)
             t.hi[k] = __shfl_up_sync(full, r.hi[k], o);
             t.s[k] = __shfl_up_sync(full, r.s[k], o);
         }
-        if (lane - o >= head)
+        const int tl = __shfl_up_sync(full, len, o);
+        if (lane - o >= head) {
             estat_merge(r, t);
+            len += tl;
+        }
     }
-    len = lane - head + 1;
     const int nextKey = __shfl_down_sync(full, key, 1);
     return lane == 31 || nextKey != key;
 }
 
-// merges a run's box and sum into a node (global or shared); sums add as two's complement
-template <class Stat>
-__device__ __forceinline__ void stat_atomic_box(Stat &dst, const EStat &e)
+// Merges a run's box and sum into an accumulator; sums add as two's complement. A box bound only moves one
+// way, so a bound that the stored value already beats needs no atomic (a stale read only costs one).
+__device__ __forceinline__ void stat_atomic(RStat &dst, const EStat &e, int len)
 {
+    // all six reads in flight together; plain loads, since the accumulator may live in shared memory
+    unsigned long long curLo[3], curHi[3];
     for (int k = 0; k < 3; ++k) {
-        atomicMin(&dst.lo[k], e.lo[k]);
-        atomicMax(&dst.hi[k], e.hi[k]);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&dst.sum[k]), (unsigned long long)e.s[k]);
+        curLo[k] = dst.lo[k];
+        curHi[k] = dst.hi[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (e.lo[k] < curLo[k])
+            atomicMin(&dst.lo[k], e.lo[k]);
+        if (e.hi[k] > curHi[k])
+            atomicMax(&dst.hi[k], e.hi[k]);
+        if (e.s[k] != 0)
+            atomicAdd(reinterpret_cast<unsigned long long *>(&dst.sum[k]), (unsigned long long)e.s[k]);
+    }
+    atomicAdd(&dst.count, len);
+}
+
+// Groups the warp's lanes by key (bitonic sort of (key, lane) over the 32 lanes, then every lane fetches the
+// statistics of the lane it now stands for) and reduces each group: afterwards the last lane of each group
+// holds the group's total, its key in `key` and its member count in `len`, and the function returns true
+// there. Keys may arrive in any order. All 32 lanes must call it.
+__device__ __forceinline__ bool warp_group_reduce(int &key, EStat &e, int &len)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    int k = key, src = lane;
+    for (int size = 2; size <= 32; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int ok = __shfl_xor_sync(full, k, stride);
+            const int os = __shfl_xor_sync(full, src, stride);
+            const bool ascending = (lane & size) == 0 || size == 32;
+            const bool lower = (lane & stride) == 0;
+            const bool mineFirst = k < ok || (k == ok && src < os);
+            if (mineFirst != (lower == ascending)) {
+                k = ok;
+                src = os;
+            }
+        }
+    EStat g;
+    for (int q = 0; q < 3; ++q) {
+        g.lo[q] = __shfl_sync(full, e.lo[q], src);
+        g.hi[q] = __shfl_sync(full, e.hi[q], src);
+        g.s[q] = __shfl_sync(full, e.s[q], src);
+    }
+    int l = __shfl_sync(full, len, src);
+    const bool tail = warp_segment_reduce(k, g, l);
+    key = k;
+    e = g;
+    len = l;
+    return tail;
+}
+
+// Warp reduction by key: when the keys already arrive in a few runs (the usual case in Morton order) a
+// segmented reduction suffices; a warp with many key changes groups its lanes first. Returns true on the
+// lane holding a group's total (its key in `key`, its member count in `len`).
+__device__ __forceinline__ bool warp_reduce_by_key(int &key, EStat &e, int &len)
+{
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+    const unsigned changes = __ballot_sync(0xFFFFFFFFu, lane > 0 && prev != key);
+    if (__popc(changes) > 3)
+        return warp_group_reduce(key, e, len);
+    return warp_segment_reduce(key, e, len);
+}
+
+// Block-level reduce-by-key. Every warp's group totals are compacted, in lane order, into shared memory;
+// warp 0 merges neighbouring entries of equal key and issues one accumulator update per merged run.
+// Entries past the shared capacity update their accumulator directly. All threads of the block must call
+// it; `target(key)` names the accumulator of a key.
+constexpr int kRunCap = 64;
+struct RunRec {
+    int key, len;
+    EStat e;
+};
+
+__device__ __forceinline__ void estat_neutral(EStat &e)
+{
+    for (int q = 0; q < 3; ++q) {
+        e.lo[q] = ~0ull;
+        e.hi[q] = 0ull;
+        e.s[q] = 0;
     }
 }
 
-__device__ __forceinline__ void stat_atomic(RStat &dst, const EStat &e, int len)
+template <class Target>
+__device__ __forceinline__ void block_reduce_keys(int key, EStat e, int len, RunRec *runs, int *warpRuns,
+                                                  Target target)
 {
-    stat_atomic_box(dst, e);
-    atomicAdd(&dst.count, len);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const bool mine = warp_reduce_by_key(key, e, len) && key >= 0;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, mine);
+    if (lane == 0)
+        warpRuns[w] = __popc(bal);
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int i = 0; i < nw; ++i) {
+        const int c = warpRuns[i];
+        off += i < w ? c : 0;
+        total += c;
+    }
+    const int idx = off + __popc(bal & ((1u << lane) - 1u));
+    if (mine) {
+        if (idx < kRunCap) {
+            runs[idx].key = key;
+            runs[idx].len = len;
+            runs[idx].e = e;
+        } else {
+            stat_atomic(target(key), e, len);
+        }
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nr = total < kRunCap ? total : kRunCap;
+        for (int b = 0; b < nr; b += 32) {
+            const int j = b + lane;
+            const bool v = j < nr;
+            int k2 = v ? runs[j].key : -1;
+            int l2 = v ? runs[j].len : 0;
+            EStat e2;
+            if (v)
+                e2 = runs[j].e;
+            else
+                estat_neutral(e2);
+            if (warp_segment_reduce(k2, e2, l2) && k2 >= 0)
+                stat_atomic(target(k2), e2, l2);
+        }
+    }
+    __syncthreads();
 }
 
 // block-wide exclusive scan of one int per thread (blockDim.x a multiple of 32, at most 1024)
@@ -262,33 +392,40 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int &total, int *warp
 // ---------------------------------------------------------------------------------------------------
 // Root: records, box, grid exponents, fixed-point sum, split parameters
 // ---------------------------------------------------------------------------------------------------
-__global__ void k_rr_init(RNode *nodes, int nt, int *counters)
+constexpr int kElemThreads = 256; // block size of the per-member passes
+
+__device__ __forceinline__ void node_clear(RNode &r, int begin, int count, int dir)
 {
-    RNode &r = nodes[0];
-    r.begin = 0;
-    r.count = nt;
-    r.child = -1;
-    r.dir = 0;
-    r.axis = 0;
+    r.begin = begin;
+    r.count = count;
+    r.dir = dir;
     r.flags = 0;
     r.mode = 0;
-    r.pad = 0;
-    r.clo = r.chi = 0;
+    r.pad[0] = r.pad[1] = r.pad[2] = 0;
     rstat_clear(r.st);
     rstat_clear(r.acc[0]);
     rstat_clear(r.acc[1]);
-    r.st.count = nt;
+    r.st.count = count;
+}
+
+__global__ void k_rr_init(RNode *nodes, NParam *np, int nt, int *counters)
+{
+    node_clear(nodes[0], 0, nt, 0);
+    np[0] = NParam{-1, nt, 0, 0, 0ull, 0ull};
     for (int i = 0; i < kCtCount; ++i)
         counters[i] = 0;
     counters[kCtNodes] = 1;
 }
 
-// box centre of each triangle as AxisAlignedBoudingBox::updateCenter computes it, (((0 + v0) + v1) + v2) /
-// (float)3 (src/axisalignedboundingbox.h:31-53), its box, and the root box (src/solidmesh.cpp:68-72)
-__global__ void __launch_bounds__(kWide) k_rr_elems(int nt, const double *__restrict__ v,
-                                                    const uint32_t *__restrict__ t,
-                                                    const double *__restrict__ box64, RRec *rec, int *nodeOf,
-                                                    int8_t *side, RNode *nodes)
+// Box centre of each triangle as AxisAlignedBoudingBox::updateCenter computes it, (((0 + v0) + v1) + v2) /
+// (float)3 (src/axisalignedboundingbox.h:31-53), its box, and the root box (src/solidmesh.cpp:68-72).
+// Records are stored in Morton order (position p holds triangle leafTri[p]): member order is carried by the
+// direction bits, so the processing order is free, and in Morton order a node's members form long runs.
+__global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double *__restrict__ v,
+                                                           const uint32_t *__restrict__ t,
+                                                           const double *__restrict__ box64,
+                                                           const int *__restrict__ leafTri, RRec *rec, int *posOf,
+                                                           int *state, RNode *nodes)
 {
     __shared__ unsigned long long sLo[3], sHi[3];
     if (threadIdx.x < 3) {
@@ -296,23 +433,24 @@ __global__ void __launch_bounds__(kWide) k_rr_elems(int nt, const double *__rest
         sHi[threadIdx.x] = 0ull;
     }
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
-    if (i < nt) {
+    if (p < nt) {
+        const int i = leafTri[p];
         RRec r;
         for (int a = 0; a < 3; ++a) {
             double s = 0.0;
             for (int k = 0; k < 3; ++k)
                 s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
-            r.c[a] = s / 3.0;
+            r.c[a] = div3_rn(s);
             r.lo[a] = box64[6 * (size_t)i + a];
             r.hi[a] = box64[6 * (size_t)i + 3 + a];
             lo[a] = ordc(r.lo[a]);
             hi[a] = ordc(r.hi[a]);
         }
-        rec[i] = r;
-        nodeOf[i] = 0;
-        side[i] = -1;
+        rec[p] = r;
+        posOf[i] = p;
+        state[p] = 0;
     }
     for (int o = 16; o > 0; o >>= 1)
         for (int a = 0; a < 3; ++a) {
@@ -331,8 +469,8 @@ __global__ void __launch_bounds__(kWide) k_rr_elems(int nt, const double *__rest
     }
 }
 
-__global__ void __launch_bounds__(kWide) k_rr_root_sum(int nt, const RRec *__restrict__ rec, RNode *nodes,
-                                                       int *scg)
+__global__ void __launch_bounds__(kElemThreads) k_rr_root_sum(int nt, const RRec *__restrict__ rec, RNode *nodes,
+                                                              int *scg)
 {
     __shared__ long long sSum[3];
     __shared__ int sc[3];
@@ -362,11 +500,13 @@ __global__ void __launch_bounds__(kWide) k_rr_root_sum(int nt, const RRec *__res
                   (unsigned long long)sSum[threadIdx.x]);
 }
 
-__global__ void k_rr_root_params(RNode *nodes, int nt, const int *scg, int *counters, int *terms)
+__global__ void k_rr_root_params(RNode *nodes, NParam *np, int nt, const int *scg, int *counters, int *terms)
 {
     RNode &r = nodes[0];
     if (nt > kSub) {
-        node_params(r.st.lo, r.st.hi, r.st.sum, nt, scg, r.axis, r.clo, r.chi);
+        NParam q{-1, nt, 0, 0, 0ull, 0ull};
+        node_params(r.st.lo, r.st.hi, r.st.sum, nt, scg, q.axis, q.clo, q.chi);
+        np[0] = q;
         counters[kCtFirst] = 0;
         counters[kCtLast] = 1;
     } else {
@@ -378,236 +518,249 @@ __global__ void k_rr_root_params(RNode *nodes, int nt, const int *scg, int *coun
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Large-node phase, one level per (classify, resolve, children)
+// Large-node phase, one level per (classify, children)
 // ---------------------------------------------------------------------------------------------------
 
 // Moves every member decided at the previous level into its child, then classifies the members of this
-// level's large nodes against their intervals and accumulates the children's statistics. side[i]: -1 none
-// pending, 0 left, 1 right, 2 inside the interval (resolved exactly by k_rr_resolve).
-__global__ void __launch_bounds__(kWide) k_rr_classify(int nt, const int *__restrict__ counters,
-                                                       const RRec *__restrict__ rec, int *nodeOf, int8_t *side,
-                                                       RNode *nodes, const int *__restrict__ scg)
+// level's large nodes against their intervals and accumulates the children's statistics. Indexed by Morton
+// position.
+__global__ void __launch_bounds__(kElemThreads, 4) k_rr_classify(int nt, const int *__restrict__ counters,
+                                                                 const RRec *__restrict__ rec, int *state,
+                                                                 const NParam *__restrict__ np, RNode *nodes,
+                                                                 const int *__restrict__ scg)
 {
-    constexpr int kTab = 64; // per-block table for levels with at most 32 nodes
-    __shared__ RStat tab[kTab];
-    __shared__ int sc[3];
+    __shared__ RunRec runs[kRunCap];
+    __shared__ int warpRuns[kElemThreads / 32];
     const int first = counters[kCtFirst], last = counters[kCtLast];
     if (first >= last)
         return;
-    const bool small = last - first <= kTab / 2;
-    if (threadIdx.x < 3)
-        sc[threadIdx.x] = scg[threadIdx.x];
-    if (small)
-        for (int j = threadIdx.x; j < kTab; j += blockDim.x)
-            rstat_clear(tab[j]);
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sc[3] = {scg[0], scg[1], scg[2]};
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    RRec r;
+    if (p < nt)
+        r = rec[p];
     int key = -1;
-    if (i < nt) {
-        int p = nodeOf[i];
-        const int s = side[i];
-        if (s >= 0) {
-            const int c = nodes[p].child;
-            if (c >= 0) {
-                p = c + s;
-                nodeOf[i] = p;
-            }
-            side[i] = -1;
+    if (p < nt) {
+        const int v = state[p];
+        int node = st_node(v), tag = st_tag(v);
+        if (tag == 1 || tag == 2) {
+            const int c = np[node].child;
+            if (c >= 0)
+                node = c + tag - 1;
+            tag = 0;
         }
-        if (p >= first && p < last) {
-            const RNode &nd = nodes[p];
-            if (nd.count > kSub) {
-                const unsigned long long o = ordc(rec[i].c[nd.axis]);
-                const int sd = o < nd.clo ? 0 : (o >= nd.chi ? 1 : 2);
-                side[i] = (int8_t)sd;
+        if (node >= first && node < last) {
+            const NParam q = np[node];
+            if (q.count > kSub) {
+                const double c = q.axis == 0 ? r.c[0] : (q.axis == 1 ? r.c[1] : r.c[2]); // no local array
+                const unsigned long long o = ordc(c);
+                const int sd = o < q.clo ? 0 : (o >= q.chi ? 1 : 2);
+                tag = sd + 1;
                 if (sd == 2)
-                    atomicOr(&nodes[p].flags, 1);
+                    atomicOr(&nodes[node].flags, 1);
                 else
-                    key = (p - first) * 2 + sd;
+                    key = (node - first) * 2 + sd;
             }
         }
+        const int nv = (node << 2) | tag;
+        if (nv != v)
+            state[p] = nv;
     }
-    EStat e = estat_of(key >= 0, rec[i < nt ? i : 0], sc);
-    int len = 0;
-    const bool tail = warp_segment_reduce(key, e, len);
-    if (small) {
-        if (tail && key >= 0)
-            stat_atomic(tab[key], e, len);
-        __syncthreads();
-        for (int j = threadIdx.x; j < 2 * (last - first); j += blockDim.x)
-            if (tab[j].count > 0) {
-                EStat t;
-                for (int k = 0; k < 3; ++k) {
-                    t.lo[k] = tab[j].lo[k];
-                    t.hi[k] = tab[j].hi[k];
-                    t.s[k] = tab[j].sum[k];
-                }
-                stat_atomic(nodes[first + (j >> 1)].acc[j & 1], t, tab[j].count);
-            }
-    } else if (tail && key >= 0) {
-        stat_atomic(nodes[first + (key >> 1)].acc[key & 1], e, len);
-    }
+    const EStat e = estat_of(key >= 0, r, sc);
+    block_reduce_keys(key, e, key >= 0 ? 1 : 0, runs, warpRuns,
+                      [&](int k) -> RStat & { return nodes[first + (k >> 1)].acc[k & 1]; });
 }
 
-// Nodes that need their member order: a member inside the interval (the reference's sequential sum in member
-// order decides), or an empty side (the split takes halves of the member order). One block per such node
-// lists its members by triangle index, then rewrites their sides and the children's statistics. Rare.
-__global__ void __launch_bounds__(kWide) k_rr_resolve(int nt, int *counters, const RRec *__restrict__ rec,
-                                                      const int *__restrict__ nodeOf, int8_t *side, RNode *nodes,
-                                                      int *pool, const int *__restrict__ scg)
+// Exact sides of one node whose member order matters: a member inside the interval (the reference's
+// sequential sum in member order decides), or an empty side (the split takes halves of the member order).
+// Run by the whole block; lists the members by triangle index, rewrites their state words and the children's
+// statistics. Rare.
+__device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *state, const NParam &q,
+                             RNode &nd, int *list, const int *__restrict__ posOf, const int *sc, int *warpSums,
+                             RunRec *runs, RStat *sAcc, int &sLeft, double &sSplit)
 {
-    __shared__ int warpSums[32];
-    __shared__ int sOff, sLeft;
-    __shared__ double sSplit;
-    __shared__ RStat sAcc[2];
-    const int first = counters[kCtFirst], last = counters[kCtLast];
     const int tid = threadIdx.x;
-    int sc[3] = {scg[0], scg[1], scg[2]};
-    for (int id = first + blockIdx.x; id < last; id += gridDim.x) {
-        RNode &nd = nodes[id];
-        const int n = nd.count;
-        if (n <= kSub)
-            continue;
-        const bool amb = (nd.flags & 1) != 0;
-        if (!amb && nd.acc[0].count > 0 && nd.acc[1].count > 0)
-            continue;
-        // members by ascending triangle index
+    const int n = q.count;
+    const bool amb = (nd.flags & 1) != 0;
+    if (tid == 0)
+        sLeft = 0;
+    int got = 0;
+    for (int b = 0; b < nt; b += blockDim.x) {
+        const int i = b + tid; // triangle index
+        const int pos = i < nt ? posOf[i] : 0;
+        const int m = (i < nt && st_node(state[pos]) == id) ? 1 : 0;
+        int tot;
+        const int at = block_exclusive_scan(m, tot, warpSums);
+        if (m && got + at < n)
+            list[got + at] = pos;
+        got += tot;
+    }
+    const int dir = nd.dir, axis = q.axis;
+    if (amb) {
         if (tid == 0) {
-            sOff = atomicAdd(counters + kCtPool, n);
-            sLeft = 0;
+            double s = 0.0;
+            for (int k = 0; k < n; ++k)
+                s = s + rec[list[dir ? n - 1 - k : k]].c[axis];
+            sSplit = s / (double)(float)n;
         }
-        __syncthreads();
-        int *list = pool + sOff;
-        int got = 0;
-        for (int b = 0; b < nt; b += blockDim.x) {
-            const int i = b + tid;
-            const int m = (i < nt && nodeOf[i] == id) ? 1 : 0;
-            int tot;
-            const int pos = block_exclusive_scan(m, tot, warpSums);
-            if (m && got + pos < n)
-                list[got + pos] = i;
-            got += tot;
-        }
-        const int dir = nd.dir, axis = nd.axis;
-        if (amb) {
-            if (tid == 0) {
-                double s = 0.0;
-                for (int k = 0; k < n; ++k)
-                    s = s + rec[list[dir ? n - 1 - k : k]].c[axis];
-                sSplit = s / (double)(float)n;
-            }
-            __syncthreads();
-        }
-        // exact sides; count the left ones
-        int myLeft = 0;
-        for (int k = tid; k < n; k += blockDim.x) {
-            const double c = rec[list[k]].c[axis];
-            const bool left = amb ? (c < sSplit) : (ordc(c) < nd.clo);
-            myLeft += left ? 1 : 0;
-        }
-        for (int o = 16; o > 0; o >>= 1)
-            myLeft += __shfl_xor_sync(0xFFFFFFFFu, myLeft, o);
-        if ((tid & 31) == 0)
-            atomicAdd(&sLeft, myLeft);
-        if (tid < 2)
-            rstat_clear(sAcc[tid]);
-        __syncthreads();
-        const int L = sLeft;
-        const int mode = L == 0 ? 1 : (L == n ? 2 : 0);
-        for (int k0 = 0; k0 < n; k0 += blockDim.x) {
-            const int k = k0 + tid;
-            int sd = -1;
-            if (k < n) {
-                const int i = list[k];
-                const int mp = dir ? n - 1 - k : k; // position in member order
-                if (mode == 0) {
-                    const double c = rec[i].c[axis];
-                    sd = (amb ? (c < sSplit) : (ordc(c) < nd.clo)) ? 0 : 1;
-                } else if (mode == 1) {
-                    sd = mp < n / 2 ? 0 : 1;                  // all right, in member order: halves
-                } else {
-                    sd = (n - 1 - mp) < n - n / 2 ? 0 : 1;    // all left, reversed: halves
-                }
-                side[i] = (int8_t)sd;
-            }
-            // per-side statistics (list order is by index, so runs of equal side are common)
-            EStat e = estat_of(sd >= 0, rec[k < n ? list[k] : 0], sc);
-            int len = 0;
-            if (warp_segment_reduce(sd, e, len) && sd >= 0)
-                stat_atomic(sAcc[sd], e, len);
-        }
-        __syncthreads();
-        if (tid < 2)
-            nd.acc[tid] = sAcc[tid];
-        if (tid == 0)
-            nd.mode = mode;
         __syncthreads();
     }
+    int myLeft = 0;
+    for (int k = tid; k < n; k += blockDim.x) {
+        const double c = rec[list[k]].c[axis];
+        myLeft += (amb ? (c < sSplit) : (ordc(c) < q.clo)) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        myLeft += __shfl_xor_sync(0xFFFFFFFFu, myLeft, o);
+    if ((tid & 31) == 0)
+        atomicAdd(&sLeft, myLeft);
+    if (tid < 2)
+        rstat_clear(sAcc[tid]);
+    __syncthreads();
+    const int L = sLeft;
+    const int mode = L == 0 ? 1 : (L == n ? 2 : 0);
+    for (int k0 = 0; k0 < n; k0 += blockDim.x) {
+        const int k = k0 + tid;
+        int sd = -1;
+        if (k < n) {
+            const int pos = list[k];
+            const int mp = dir ? n - 1 - k : k; // position in member order
+            if (mode == 0) {
+                const double c = rec[pos].c[axis];
+                sd = (amb ? (c < sSplit) : (ordc(c) < q.clo)) ? 0 : 1;
+            } else if (mode == 1) {
+                sd = mp < n / 2 ? 0 : 1;               // all right, in member order: halves
+            } else {
+                sd = (n - 1 - mp) < n - n / 2 ? 0 : 1; // all left, reversed: halves
+            }
+            state[pos] = (id << 2) | (sd + 1);
+        }
+        const EStat e = estat_of(sd >= 0, rec[k < n ? list[k] : 0], sc);
+        block_reduce_keys(sd, e, sd >= 0 ? 1 : 0, runs, warpSums, [&](int qq) -> RStat & { return sAcc[qq]; });
+    }
+    if (tid < 2)
+        nd.acc[tid] = sAcc[tid];
+    if (tid == 0) {
+        nd.mode = mode;
+        nd.flags = 0;
+    }
+    __syncthreads();
 }
 
-// One block: allocates the children of every node split at this level, fills their statistics and split
-// parameters, lists the terminal ones, and advances the level bounds.
-__global__ void __launch_bounds__(kWide) k_rr_children(RNode *nodes, int *counters, int *terms, int maxNodes,
+// One block per level: resolves the rare nodes that need their member order, allocates the children of every
+// node split at this level (block scans, no atomics), fills their statistics and split parameters, lists the
+// terminal ones, and advances the level bounds.
+__global__ void __launch_bounds__(kWide) k_rr_children(int nt, RNode *nodes, NParam *np, int *counters, int *terms,
+                                                       int maxNodes, const RRec *__restrict__ rec, int *state,
+                                                       const int *__restrict__ posOf, int *pool,
                                                        const int *__restrict__ scg)
 {
+    __shared__ int warpSums[32];
+    __shared__ RunRec runs[kRunCap];
+    __shared__ RStat sAcc[2];
+    __shared__ int sLeft, nFlag;
+    __shared__ double sSplit;
+    __shared__ int flagged[kWide];
     const int first = counters[kCtFirst], last = counters[kCtLast];
     if (first >= last)
         return;
-    int sc[3] = {scg[0], scg[1], scg[2]};
-    for (int id = first + threadIdx.x; id < last; id += blockDim.x) {
-        RNode &nd = nodes[id];
-        if (nd.count <= kSub)
-            continue;
-        const int c = atomicAdd(counters + kCtNodes, 2);
-        if (c + 2 > maxNodes) {
-            atomicAdd(counters + kCtOverflow, 1); // nothing is split further; the host reports the overflow
-            continue;
+    const int tid = threadIdx.x;
+    const int sc[3] = {scg[0], scg[1], scg[2]};
+    // nodes that need the exact, order-aware resolution
+    for (int b = first; b < last; b += kWide) {
+        if (tid == 0)
+            nFlag = 0;
+        __syncthreads();
+        const int id = b + tid;
+        if (id < last) {
+            const RNode &nd = nodes[id];
+            if (nd.count > kSub && ((nd.flags & 1) || nd.acc[0].count == 0 || nd.acc[1].count == 0))
+                flagged[atomicAdd(&nFlag, 1)] = id;
         }
-        const int mode = nd.mode, dir = nd.dir;
-        const int dl = mode == 1 ? dir : dir ^ 1;
-        const int dr = mode == 2 ? dir ^ 1 : dir;
-        for (int s = 0; s < 2; ++s) {
-            RNode &ch = nodes[c + s];
-            ch.begin = s == 0 ? nd.begin : nd.begin + nd.acc[0].count;
-            ch.count = nd.acc[s].count;
-            ch.child = -1;
-            ch.dir = s == 0 ? dl : dr;
-            ch.axis = 0;
-            ch.flags = 0;
-            ch.mode = 0;
-            ch.pad = 0;
-            ch.st = nd.acc[s];
-            rstat_clear(ch.acc[0]);
-            rstat_clear(ch.acc[1]);
-            if (ch.count > kSub)
-                node_params(ch.st.lo, ch.st.hi, ch.st.sum, ch.count, sc, ch.axis, ch.clo, ch.chi);
-            else
-                terms[atomicAdd(counters + kCtTerms, 1)] = c + s;
+        __syncthreads();
+        const int nf = nFlag;
+        for (int f = 0; f < nf; ++f) {
+            const int fid = flagged[f];
+            const NParam q = np[fid];
+            resolve_node(fid, nt, rec, state, q, nodes[fid], pool, posOf, sc, warpSums, runs, sAcc, sLeft, sSplit);
         }
-        nd.child = c;
+        __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    // children
+    int nodeBase = counters[kCtNodes], termBase = counters[kCtTerms];
+    bool overflow = false;
+    for (int b = first; b < last; b += kWide) {
+        const int id = b + tid;
+        const RNode *nd = id < last ? &nodes[id] : nullptr;
+        const int split = (nd && nd->count > kSub) ? 1 : 0;
+        int totSplit;
+        const int at = block_exclusive_scan(split, totSplit, warpSums);
+        const int c = nodeBase + 2 * at;
+        const bool ok = split && c + 2 <= maxNodes;
+        overflow |= split && !ok;
+        int nTerm = 0, cnt[2] = {0, 0};
+        if (ok) {
+            const int mode = nd->mode, dir = nd->dir;
+            const int dl = mode == 1 ? dir : dir ^ 1;
+            const int dr = mode == 2 ? dir ^ 1 : dir;
+            for (int s2 = 0; s2 < 2; ++s2) {
+                cnt[s2] = nd->acc[s2].count;
+                RNode &ch = nodes[c + s2];
+                ch.begin = s2 == 0 ? nd->begin : nd->begin + nd->acc[0].count;
+                ch.count = cnt[s2];
+                ch.dir = s2 == 0 ? dl : dr;
+                ch.flags = 0;
+                ch.mode = 0;
+                ch.pad[0] = ch.pad[1] = ch.pad[2] = 0;
+                ch.st = nd->acc[s2];
+                rstat_clear(ch.acc[0]);
+                rstat_clear(ch.acc[1]);
+                NParam cq{-1, cnt[s2], 0, 0, 0ull, 0ull};
+                if (cnt[s2] > kSub)
+                    node_params(ch.st.lo, ch.st.hi, ch.st.sum, cnt[s2], sc, cq.axis, cq.clo, cq.chi);
+                else
+                    ++nTerm;
+                np[c + s2] = cq;
+            }
+            np[id].child = c;
+        }
+        int totTerm;
+        const int tat = block_exclusive_scan(nTerm, totTerm, warpSums);
+        if (ok) {
+            int t2 = termBase + tat;
+            for (int s2 = 0; s2 < 2; ++s2)
+                if (cnt[s2] <= kSub)
+                    terms[t2++] = c + s2;
+        }
+        nodeBase += 2 * totSplit;
+        termBase += totTerm;
+    }
+    overflow = __syncthreads_or(overflow);
+    if (tid == 0) {
+        counters[kCtNodes] = nodeBase < maxNodes ? nodeBase : maxNodes;
+        counters[kCtTerms] = termBase;
+        if (overflow)
+            counters[kCtOverflow] = 1;
         counters[kCtFirst] = last;
-        counters[kCtLast] = counters[kCtNodes];
-        counters[kCtPool] = 0;
+        counters[kCtLast] = overflow ? last : counters[kCtNodes];
     }
 }
 
-// after the last level: every member's terminal node and the sort key (the node's first leaf position)
-__global__ void k_rr_finish(int nt, int *nodeOf, int8_t *side, const RNode *__restrict__ nodes, int *key,
-                            int *val)
+// After the last level: every member's terminal node, and the sort key (the node's first leaf position)
+// stored by triangle index, so that a stable sort lists each node's members by ascending index.
+__global__ void k_rr_finish(int nt, const int *__restrict__ state, const NParam *__restrict__ np,
+                            const RNode *__restrict__ nodes, const int *__restrict__ leafTri, int *key, int *val)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nt)
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nt)
         return;
-    int p = nodeOf[i];
-    const int s = side[i];
-    if (s >= 0 && nodes[p].child >= 0) {
-        p = nodes[p].child + s;
-        nodeOf[i] = p;
-    }
-    key[i] = nodes[p].begin;
+    const int v = state[q];
+    int node = st_node(v);
+    const int tag = st_tag(v);
+    if ((tag == 1 || tag == 2) && np[node].child >= 0)
+        node = np[node].child + tag - 1;
+    const int i = leafTri[q];
+    key[i] = nodes[node].begin;
     val[i] = i;
 }
 
@@ -643,7 +796,8 @@ constexpr size_t kSubSmem = sizeof(SNode) * kSubNodes + sizeof(int) * (6 * kSub 
 
 __global__ void __launch_bounds__(kSubThreads)
     k_rr_subtree(const int *__restrict__ terms, const RNode *__restrict__ gnodes, const int *__restrict__ sorted,
-                 const RRec *__restrict__ rec, const int *__restrict__ scg, int *rank, int *counters)
+                 const RRec *__restrict__ rec, const int *__restrict__ posOf, const int *__restrict__ leafTri,
+                 const int *__restrict__ scg, int *rank, int *counters)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     SNode *nodes = reinterpret_cast<SNode *>(smem);
@@ -657,14 +811,15 @@ __global__ void __launch_bounds__(kSubThreads)
     const RNode &g = gnodes[terms[blockIdx.x]];
     const int base = g.begin, n = g.count, dir = g.dir;
     int sc[3] = {scg[0], scg[1], scg[2]};
+    // perm holds Morton positions (record indices), in member order
     for (int p = tid; p < n; p += kSubThreads) {
-        perm[0][p] = sorted[base + (dir ? n - 1 - p : p)];
+        perm[0][p] = posOf[sorted[base + (dir ? n - 1 - p : p)]];
         nodeOf[0][p] = 0;
     }
     if (n <= kLeaf) {
         __syncthreads();
         for (int p = tid; p < n; p += kSubThreads)
-            rank[perm[0][p]] = base + p;
+            rank[leafTri[perm[0][p]]] = base + p;
         return;
     }
     if (tid == 0) {
@@ -811,16 +966,44 @@ __global__ void __launch_bounds__(kSubThreads)
             nodeOf[cur ^ 1][q] = nodes[ch].count > kLeaf ? ch : -2; // leaves need no statistics
         }
         __syncthreads();
-        // statistics of the children that split again, read in the new order (members of a node are
-        // contiguous, so the warp reduction sees runs)
+        // Statistics of the children that split again, read in the new order. A node's members are
+        // contiguous, so each warp's runs end either at a node's last member (that run's total goes to the
+        // node) or at the warp's last lane (kept per 32-position chunk); one thread per node then adds the
+        // chunk totals inside its range. No atomics.
+        EStat *chunk = reinterpret_cast<EStat *>(scan); // the scan is consumed; kSub / 32 entries fit
         for (int p0 = 0; p0 < n; p0 += kSubThreads) {
             const int p = p0 + tid;
             const int id = p < n ? nodeOf[cur ^ 1][p] : -1;
             const int key = id >= 0 ? id : -1;
             EStat e = estat_of(key >= 0, rec[key >= 0 ? perm[cur ^ 1][p] : 0], sc);
-            int len = 0;
-            if (warp_segment_reduce(key, e, len) && key >= 0)
-                stat_atomic_box(nodes[key], e);
+            int len = 1;
+            if (warp_segment_reduce(key, e, len) && key >= 0) {
+                SNode &nd = nodes[key];
+                if (p == nd.begin + nd.count - 1) {
+                    for (int k = 0; k < 3; ++k) {
+                        nd.lo[k] = e.lo[k];
+                        nd.hi[k] = e.hi[k];
+                        nd.sum[k] = e.s[k];
+                    }
+                } else {
+                    chunk[p >> 5] = e; // p is the last position of its chunk
+                }
+            }
+        }
+        __syncthreads();
+        for (int id = last + tid; id < nNodes; id += kSubThreads) {
+            SNode &nd = nodes[id];
+            if (nd.count <= kLeaf)
+                continue;
+            const int b = nd.begin, e = nd.begin + nd.count - 1; // chunk ends in [b, e) belong to the node
+            for (int j = b >> 5; 32 * j + 31 < e; ++j) { // 32 (b / 32) + 31 is the first chunk end >= b
+                const EStat &c = chunk[j];
+                for (int k = 0; k < 3; ++k) {
+                    nd.lo[k] = min(nd.lo[k], c.lo[k]);
+                    nd.hi[k] = max(nd.hi[k], c.hi[k]);
+                    nd.sum[k] += c.s[k];
+                }
+            }
         }
         __syncthreads();
         if (tid == 0) {
@@ -833,7 +1016,7 @@ __global__ void __launch_bounds__(kSubThreads)
     if (tid == 0 && (err || lFirst < lLast))
         atomicAdd(counters + kCtSubErr, 1);
     for (int p = tid; p < n; p += kSubThreads)
-        rank[perm[cur][p]] = base + p;
+        rank[leafTri[perm[cur][p]]] = base + p;
 }
 
 static int bit_length(int x)
@@ -861,26 +1044,27 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, (int *)nullptr, (int *)nullptr, (int *)nullptr,
                                     (int *)nullptr, nt, 0, keyBits, s);
     Carve c;
-    const size_t o_rec = c.take<RRec>(nt), o_nodeOf = c.take<int>(nt), o_side = c.take<int8_t>(nt);
+    const size_t o_rec = c.take<RRec>(nt), o_state = c.take<int>(nt), o_pos = c.take<int>(nt);
     const size_t o_key = c.take<int>(nt), o_val = c.take<int>(nt), o_skey = c.take<int>(nt),
                  o_sval = c.take<int>(nt), o_pool = c.take<int>(nt);
+    const size_t o_np = c.take<NParam>(maxNodes);
     const size_t o_nodes = c.take<RNode>(maxNodes), o_terms = c.take<int>(maxNodes), o_ct = c.take<int>(kCtCount),
                  o_sc = c.take<int>(4), o_cub = c.take<char>(sortBytes);
     SB_CUDA_CHECK(m->tmp.ensure(c.off));
     char *b = m->tmp.as<char>();
     RRec *rec = (RRec *)(b + o_rec);
-    int *nodeOf = (int *)(b + o_nodeOf);
-    int8_t *side = (int8_t *)(b + o_side);
+    int *state = (int *)(b + o_state);
+    NParam *np = (NParam *)(b + o_np);
     int *key = (int *)(b + o_key), *val = (int *)(b + o_val), *skey = (int *)(b + o_skey), *sval = (int *)(b + o_sval);
-    int *pool = (int *)(b + o_pool);
+    int *pool = (int *)(b + o_pool), *posOf = (int *)(b + o_pos);
     RNode *nodes = (RNode *)(b + o_nodes);
     int *terms = (int *)(b + o_terms), *counters = (int *)(b + o_ct), *scg = (int *)(b + o_sc);
 
-    const int GW = (nt + kWide - 1) / kWide;
-    SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, nt, counters);
-    SB_COUNT(k_rr_elems)<<<GW, kWide, 0, s>>>(nt, d.v, d.t, d.box64, rec, nodeOf, side, nodes);
-    SB_COUNT(k_rr_root_sum)<<<GW, kWide, 0, s>>>(nt, rec, nodes, scg);
-    SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, nt, scg, counters, terms);
+    const int GE = (nt + kElemThreads - 1) / kElemThreads;
+    SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters);
+    SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, posOf, state, nodes);
+    SB_COUNT(k_rr_root_sum)<<<GE, kElemThreads, 0, s>>>(nt, rec, nodes, scg);
+    SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, np, nt, scg, counters, terms);
     // levels run in batches; the host looks at the level bounds only between batches. The first batch
     // covers the expected depth of the large-node phase (a mean split roughly halves); empty levels cost
     // only their launches.
@@ -891,9 +1075,9 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     int cnt[kCtCount] = {0};
     for (int level = 0, batch = expected + 1; level < 4096 && !done; level += batch, batch = 2) {
         for (int j = 0; j < batch; ++j) {
-            SB_COUNT(k_rr_classify)<<<GW, kWide, 0, s>>>(nt, counters, rec, nodeOf, side, nodes, scg);
-            SB_COUNT(k_rr_resolve)<<<152, kWide, 0, s>>>(nt, counters, rec, nodeOf, side, nodes, pool, scg);
-            SB_COUNT(k_rr_children)<<<1, kWide, 0, s>>>(nodes, counters, terms, maxNodes, scg);
+            SB_COUNT(k_rr_classify)<<<GE, kElemThreads, 0, s>>>(nt, counters, rec, state, np, nodes, scg);
+            SB_COUNT(k_rr_children)<<<1, kWide, 0, s>>>(nt, nodes, np, counters, terms, maxNodes, rec, state, posOf,
+                                                        pool, scg);
         }
         SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaStreamSynchronize(s));
@@ -909,10 +1093,10 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     }
     if (nt <= kSub)
         cnt[kCtTerms] = 1;
-    SB_COUNT(k_rr_finish)<<<GW, kWide, 0, s>>>(nt, nodeOf, side, nodes, key, val);
+    SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
     SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem));
-    SB_COUNT(k_rr_subtree)<<<cnt[kCtTerms], kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, scg, d.rank,
+    SB_COUNT(k_rr_subtree)<<<cnt[kCtTerms], kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri, scg, d.rank,
                                                                         counters);
     int errs = 0;
     SB_CUDA_CHECK(cudaMemcpyAsync(&errs, counters + kCtSubErr, sizeof errs, cudaMemcpyDeviceToHost, s));
