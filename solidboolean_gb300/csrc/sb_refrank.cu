@@ -29,6 +29,9 @@
 // resolution, children), visiting the triangles in the LBVH's Morton order so that a node's members form
 // long runs for the reductions; one radix sort then lists each remaining node's members in order, and one
 // block per such node finishes its subtree in shared memory and writes the final positions.
+#include <algorithm>
+#include <mutex>
+
 #include <cub/cub.cuh>
 
 #include "sb_common.cuh"
@@ -41,7 +44,6 @@ constexpr int kLeaf = 20;        // reference leaf size (src/axisalignedbounding
 constexpr int kSub = 1024;       // nodes with at most this many members finish in one block
 constexpr int kSubThreads = 256;
 constexpr int kSubNodes = 272;   // node records per subtree block (shared memory)
-constexpr int kWide = 1024;      // block size of the large-node phase
 
 // counters[] slots
 enum {
@@ -54,10 +56,13 @@ enum {
     kCtCount = 8
 };
 
-// one triangle: its box centre and box (stored by Morton position)
+// One triangle in integer form, stored by Morton position: order-preserving keys of its box centre and box
+// (centres compare with one integer comparison, boxes reduce with integer min/max; ord_to_dbl recovers the
+// exact doubles) and the fixed-point centre that node sums add up. 96 bytes, three sectors.
 struct RRec {
-    double c[3];
-    double lo[3], hi[3];
+    unsigned long long c[3];
+    unsigned long long lo[3], hi[3];
+    long long fx[3];
 };
 
 // box (order-preserving keys) and fixed-point centre sum of a set of members
@@ -180,13 +185,13 @@ struct EStat {
     long long s[3];
 };
 
-__device__ __forceinline__ EStat estat_of(bool valid, const RRec &r, const int *sc)
+__device__ __forceinline__ EStat estat_of(bool valid, const RRec &r)
 {
     EStat e;
     for (int k = 0; k < 3; ++k) {
-        e.lo[k] = valid ? ordc(r.lo[k]) : ~0ull;
-        e.hi[k] = valid ? ordc(r.hi[k]) : 0ull;
-        e.s[k] = valid ? to_fixed(r.c[k], sc[k]) : 0;
+        e.lo[k] = valid ? r.lo[k] : ~0ull;
+        e.hi[k] = valid ? r.hi[k] : 0ull;
+        e.s[k] = valid ? r.fx[k] : 0;
     }
     return e;
 }
@@ -231,23 +236,37 @@ __device__ __forceinline__ bool warp_segment_reduce(int key, EStat &r, int &len)
     return lane == 31 || nextKey != key;
 }
 
-// Merges a run's box and sum into an accumulator; sums add as two's complement. A box bound only moves one
-// way, so a bound that the stored value already beats needs no atomic (a stale read only costs one).
+// Segmented inclusive scan over the 32 lanes: a lane with `start` set begins a new segment (lane 0 must).
+__device__ __forceinline__ void warp_segmented_scan(bool start, EStat &r)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    int head = start ? lane : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int h = __shfl_up_sync(full, head, o);
+        if (lane >= o)
+            head = max(head, h);
+    }
+    for (int o = 1; o < 32; o <<= 1) {
+        EStat t;
+        for (int k = 0; k < 3; ++k) {
+            t.lo[k] = __shfl_up_sync(full, r.lo[k], o);
+            t.hi[k] = __shfl_up_sync(full, r.hi[k], o);
+            t.s[k] = __shfl_up_sync(full, r.s[k], o);
+        }
+        if (lane - o >= head)
+            estat_merge(r, t);
+    }
+}
+
+// Merges a run's box and sum into an accumulator (global or shared); sums add as two's complement. The
+// results are unused, so on global memory these are fire-and-forget reductions.
 __device__ __forceinline__ void stat_atomic(RStat &dst, const EStat &e, int len)
 {
-    // all six reads in flight together; plain loads, since the accumulator may live in shared memory
-    unsigned long long curLo[3], curHi[3];
     for (int k = 0; k < 3; ++k) {
-        curLo[k] = dst.lo[k];
-        curHi[k] = dst.hi[k];
-    }
-    for (int k = 0; k < 3; ++k) {
-        if (e.lo[k] < curLo[k])
-            atomicMin(&dst.lo[k], e.lo[k]);
-        if (e.hi[k] > curHi[k])
-            atomicMax(&dst.hi[k], e.hi[k]);
-        if (e.s[k] != 0)
-            atomicAdd(reinterpret_cast<unsigned long long *>(&dst.sum[k]), (unsigned long long)e.s[k]);
+        atomicMin(&dst.lo[k], e.lo[k]);
+        atomicMax(&dst.hi[k], e.hi[k]);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&dst.sum[k]), (unsigned long long)e.s[k]);
     }
     atomicAdd(&dst.count, len);
 }
@@ -303,7 +322,8 @@ __device__ __forceinline__ bool warp_reduce_by_key(int &key, EStat &e, int &len)
 // Block-level reduce-by-key. Every warp's group totals are compacted, in lane order, into shared memory;
 // warp 0 merges neighbouring entries of equal key and issues one accumulator update per merged run.
 // Entries past the shared capacity update their accumulator directly. All threads of the block must call
-// it; `target(key)` names the accumulator of a key.
+// it; `target(key)` names the accumulator of a key. There is no barrier at the end: the next call's first
+// barrier orders the reuse of `runs`, and a caller that reads a shared target must synchronise first.
 constexpr int kRunCap = 64;
 struct RunRec {
     int key, len;
@@ -362,7 +382,6 @@ __device__ __forceinline__ void block_reduce_keys(int key, EStat e, int len, Run
                 stat_atomic(target(k2), e2, l2);
         }
     }
-    __syncthreads();
 }
 
 // block-wide exclusive scan of one int per thread (blockDim.x a multiple of 32, at most 1024)
@@ -408,8 +427,9 @@ __device__ __forceinline__ void node_clear(RNode &r, int begin, int count, int d
     r.st.count = count;
 }
 
-__global__ void k_rr_init(RNode *nodes, NParam *np, int nt, int *counters)
+__global__ void k_rr_init(RNode *nodes, NParam *np, int nt, int *counters, unsigned *bar)
 {
+    bar[0] = bar[1] = bar[2] = bar[3] = 0;
     node_clear(nodes[0], 0, nt, 0);
     np[0] = NParam{-1, nt, 0, 0, 0ull, 0ull};
     for (int i = 0; i < kCtCount; ++i)
@@ -424,8 +444,9 @@ __global__ void k_rr_init(RNode *nodes, NParam *np, int nt, int *counters)
 __global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double *__restrict__ v,
                                                            const uint32_t *__restrict__ t,
                                                            const double *__restrict__ box64,
-                                                           const int *__restrict__ leafTri, RRec *rec, int *posOf,
-                                                           int *state, RNode *nodes)
+                                                           const int *__restrict__ leafTri, RRec *rec,
+                                                           unsigned long long *soa, int *posOf, int *state,
+                                                           RNode *nodes)
 {
     __shared__ unsigned long long sLo[3], sHi[3];
     if (threadIdx.x < 3) {
@@ -442,11 +463,13 @@ __global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double 
             double s = 0.0;
             for (int k = 0; k < 3; ++k)
                 s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
-            r.c[a] = div3_rn(s);
-            r.lo[a] = box64[6 * (size_t)i + a];
-            r.hi[a] = box64[6 * (size_t)i + 3 + a];
-            lo[a] = ordc(r.lo[a]);
-            hi[a] = ordc(r.hi[a]);
+            r.c[a] = ordc(div3_rn(s));
+            lo[a] = r.lo[a] = ordc(box64[6 * (size_t)i + a]);
+            hi[a] = r.hi[a] = ordc(box64[6 * (size_t)i + 3 + a]);
+            r.fx[a] = 0; // filled once the grid exponents are known (k_rr_root_sum)
+            soa[(size_t)a * nt + p] = r.c[a];
+            soa[(size_t)(3 + a) * nt + p] = r.lo[a];
+            soa[(size_t)(6 + a) * nt + p] = r.hi[a];
         }
         rec[p] = r;
         posOf[i] = p;
@@ -469,8 +492,8 @@ __global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double 
     }
 }
 
-__global__ void __launch_bounds__(kElemThreads) k_rr_root_sum(int nt, const RRec *__restrict__ rec, RNode *nodes,
-                                                              int *scg)
+__global__ void __launch_bounds__(kElemThreads) k_rr_root_sum(int nt, RRec *rec, unsigned long long *soa,
+                                                              RNode *nodes, int *scg)
 {
     __shared__ long long sSum[3];
     __shared__ int sc[3];
@@ -486,8 +509,11 @@ __global__ void __launch_bounds__(kElemThreads) k_rr_root_sum(int nt, const RRec
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     long long s[3] = {0, 0, 0};
     if (i < nt)
-        for (int a = 0; a < 3; ++a)
-            s[a] = to_fixed(rec[i].c[a], sc[a]);
+        for (int a = 0; a < 3; ++a) {
+            s[a] = to_fixed(ord_to_dbl(rec[i].c[a]), sc[a]);
+            rec[i].fx[a] = s[a];
+            soa[(size_t)(9 + a) * nt + i] = (unsigned long long)s[a];
+        }
     for (int o = 16; o > 0; o >>= 1)
         for (int a = 0; a < 3; ++a)
             s[a] += __shfl_xor_sync(0xFFFFFFFFu, s[a], o);
@@ -518,97 +544,240 @@ __global__ void k_rr_root_params(RNode *nodes, NParam *np, int nt, const int *sc
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Large-node phase, one level per (classify, children)
+// Large-node phase: one persistent cooperative kernel runs every level (classify the members, grid barrier,
+// resolve and split the nodes, grid barrier). Data that other blocks write inside the kernel (member states,
+// node parameters, accumulators, counters) is read through L2 (ld.global.cg), never from a stale L1 line.
 // ---------------------------------------------------------------------------------------------------
+struct GridBar {
+    unsigned count, gen;
+    int err, pad;
+};
 
-// Moves every member decided at the previous level into its child, then classifies the members of this
-// level's large nodes against their intervals and accumulates the children's statistics. Indexed by Morton
-// position.
-__global__ void __launch_bounds__(kElemThreads, 4) k_rr_classify(int nt, const int *__restrict__ counters,
-                                                                 const RRec *__restrict__ rec, int *state,
-                                                                 const NParam *__restrict__ np, RNode *nodes,
-                                                                 const int *__restrict__ scg)
+// bounded wait: a barrier gives up and flags an error after this long (the levels take microseconds)
+constexpr unsigned long long kBarrierNs = 200ull * 1000ull * 1000ull;
+constexpr int kMaxLevels = 4096;
+
+__device__ __forceinline__ unsigned long long global_ns()
 {
-    __shared__ RunRec runs[kRunCap];
-    __shared__ int warpRuns[kElemThreads / 32];
-    const int first = counters[kCtFirst], last = counters[kCtLast];
-    if (first >= last)
-        return;
-    const int sc[3] = {scg[0], scg[1], scg[2]};
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    RRec r;
-    if (p < nt)
-        r = rec[p];
-    int key = -1;
-    if (p < nt) {
-        const int v = state[p];
-        int node = st_node(v), tag = st_tag(v);
-        if (tag == 1 || tag == 2) {
-            const int c = np[node].child;
-            if (c >= 0)
-                node = c + tag - 1;
-            tag = 0;
-        }
-        if (node >= first && node < last) {
-            const NParam q = np[node];
-            if (q.count > kSub) {
-                const double c = q.axis == 0 ? r.c[0] : (q.axis == 1 ? r.c[1] : r.c[2]); // no local array
-                const unsigned long long o = ordc(c);
-                const int sd = o < q.clo ? 0 : (o >= q.chi ? 1 : 2);
-                tag = sd + 1;
-                if (sd == 2)
-                    atomicOr(&nodes[node].flags, 1);
-                else
-                    key = (node - first) * 2 + sd;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier for a cooperative launch (every block resident). Returns false once any block gave up
+// waiting; the kernel then returns and the host reports the error.
+__device__ bool grid_sync(GridBar *gb)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &gb->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        int good = 1;
+        if (atomicAdd(&gb->count, 1u) == gridDim.x - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (*vgen == g) {
+                if (global_ns() - t0 > kBarrierNs) {
+                    atomicExch(&gb->err, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
             }
         }
-        const int nv = (node << 2) | tag;
-        if (nv != v)
-            state[p] = nv;
+        __threadfence();
+        ok = good && *reinterpret_cast<volatile int *>(&gb->err) == 0;
     }
-    const EStat e = estat_of(key >= 0, r, sc);
-    block_reduce_keys(key, e, key >= 0 ? 1 : 0, runs, warpRuns,
-                      [&](int k) -> RStat & { return nodes[first + (k >> 1)].acc[k & 1]; });
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ NParam ld_nparam(const NParam *q)
+{
+    NParam r;
+    r.child = __ldcg(&q->child);
+    r.count = __ldcg(&q->count);
+    r.axis = __ldcg(&q->axis);
+    r.pad = 0;
+    r.clo = __ldcg(&q->clo);
+    r.chi = __ldcg(&q->chi);
+    return r;
+}
+
+__device__ __forceinline__ RStat ld_rstat(const RStat *a)
+{
+    RStat r;
+    for (int k = 0; k < 3; ++k) {
+        r.lo[k] = __ldcg(&a->lo[k]);
+        r.hi[k] = __ldcg(&a->hi[k]);
+        r.sum[k] = __ldcg(&a->sum[k]);
+    }
+    r.count = __ldcg(&a->count);
+    r.pad = 0;
+    return r;
+}
+
+// Node tables of one level in shared memory: the child ids of the previous level's nodes (to move pending
+// members) and the split parameters of this level's nodes. Levels with more nodes than fit read them from
+// global memory instead.
+constexpr int kTabNodes = 1024;
+struct LevelTab {
+    int child[kTabNodes];
+    NParam par[kTabNodes];
+};
+
+__device__ __forceinline__ void load_level_tab(LevelTab &tab, const NParam *np, int prevFirst, int first, int last)
+{
+    if (first - prevFirst <= kTabNodes)
+        for (int k = threadIdx.x; k < first - prevFirst; k += blockDim.x)
+            tab.child[k] = __ldcg(&np[prevFirst + k].child);
+    if (last - first <= kTabNodes)
+        for (int k = threadIdx.x; k < last - first; k += blockDim.x)
+            tab.par[k] = ld_nparam(&np[first + k]);
+    __syncthreads();
+}
+
+// One warp walks the contiguous Morton range [wb, we) in chunks of 32 (lane = position, so every field loads
+// coalesced from the structure-of-arrays copy): moves members decided at the previous level into their child,
+// classifies the members of large nodes against their intervals, and reduces their statistics by key
+// (child, side). Keys come in long runs; a run still open at the end of a chunk is carried in lane 0 into the
+// next chunk, runs completed inside the range update their accumulators directly, and the run open at the
+// end of the range joins one block reduction. All threads of the block must call it.
+__device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, int first, int last,
+                                               const unsigned long long *__restrict__ soa, int nt, int *state,
+                                               const NParam *np, RNode *nodes, RunRec *runs, int *warpRuns,
+                                               const LevelTab &tab)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const bool childTab = first - prevFirst <= kTabNodes, parTab = last - first <= kTabNodes;
+    auto target = [&](int k) -> RStat & { return nodes[first + (k >> 1)].acc[k & 1]; };
+    int openKey = -1, openLen = 0; // lane 0's carried run
+    EStat open;
+    estat_neutral(open);
+    for (int base = wb; base < we; base += 32) {
+        const int p = base + lane;
+        int key = -1;
+        EStat e;
+        estat_neutral(e);
+        if (p < we) {
+            const int v = __ldcg(&state[p]);
+            int node = st_node(v), tag = st_tag(v);
+            if (tag == 1 || tag == 2) {
+                const int c = childTab && node >= prevFirst ? tab.child[node - prevFirst] : __ldcg(&np[node].child);
+                if (c >= 0)
+                    node = c + tag - 1;
+                tag = 0;
+            }
+            if (node >= first && node < last) {
+                const NParam q = parTab ? tab.par[node - first] : ld_nparam(&np[node]);
+                if (q.count > kSub) {
+                    const unsigned long long o = soa[(size_t)q.axis * nt + p];
+                    const int sd = o < q.clo ? 0 : (o >= q.chi ? 1 : 2);
+                    tag = sd + 1;
+                    if (sd == 2) {
+                        atomicOr(&nodes[node].flags, 1);
+                    } else {
+                        key = (node - first) * 2 + sd;
+                        for (int k = 0; k < 3; ++k) {
+                            e.lo[k] = soa[(size_t)(3 + k) * nt + p];
+                            e.hi[k] = soa[(size_t)(6 + k) * nt + p];
+                            e.s[k] = (long long)soa[(size_t)(9 + k) * nt + p];
+                        }
+                    }
+                }
+            }
+            const int nv = (node << 2) | tag;
+            if (nv != v)
+                state[p] = nv;
+        }
+        int len = key >= 0 ? 1 : 0;
+        // the carried run continues into lane 0 or is complete
+        if (lane == 0) {
+            if (openKey >= 0 && openKey == key) {
+                estat_merge(e, open);
+                len += openLen;
+            } else if (openKey >= 0) {
+                stat_atomic(target(openKey), open, openLen);
+            }
+        }
+        const int prev = __shfl_up_sync(full, key, 1);
+        const unsigned changes = __ballot_sync(full, lane > 0 && prev != key);
+        if (__popc(changes) > 3) {
+            // many short runs: group by key, flush every group, carry nothing
+            int k2 = key, l2 = len;
+            EStat e2 = e;
+            if (warp_group_reduce(k2, e2, l2) && k2 >= 0)
+                stat_atomic(target(k2), e2, l2);
+            openKey = -1;
+            openLen = 0;
+            continue;
+        }
+        const bool tail = warp_segment_reduce(key, e, len);
+        if (tail && lane != 31 && key >= 0)
+            stat_atomic(target(key), e, len); // completed inside this chunk
+        // the run through lane 31 stays open
+        const int k31 = __shfl_sync(full, key, 31);
+        const int l31 = __shfl_sync(full, len, 31);
+        EStat e31;
+        for (int k = 0; k < 3; ++k) {
+            e31.lo[k] = __shfl_sync(full, e.lo[k], 31);
+            e31.hi[k] = __shfl_sync(full, e.hi[k], 31);
+            e31.s[k] = __shfl_sync(full, e.s[k], 31);
+        }
+        openKey = k31;
+        openLen = l31;
+        open = e31;
+    }
+    // lane 0 holds the open run; it joins the block reduction
+    const int fk = lane == 0 ? openKey : -1;
+    block_reduce_keys(fk, open, lane == 0 ? openLen : 0, runs, warpRuns, target);
 }
 
 // Exact sides of one node whose member order matters: a member inside the interval (the reference's
 // sequential sum in member order decides), or an empty side (the split takes halves of the member order).
 // Run by the whole block; lists the members by triangle index, rewrites their state words and the children's
 // statistics. Rare.
-__device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *state, const NParam &q,
-                             RNode &nd, int *list, const int *__restrict__ posOf, const int *sc, int *warpSums,
-                             RunRec *runs, RStat *sAcc, int &sLeft, double &sSplit)
+__device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *state, const NParam &q, RNode &nd,
+                             int *list, const int *__restrict__ posOf, int *warpSums, RunRec *runs, RStat *sAcc,
+                             int &sLeft, double &sSplit)
 {
     const int tid = threadIdx.x;
     const int n = q.count;
-    const bool amb = (nd.flags & 1) != 0;
+    const bool amb = (__ldcg(&nd.flags) & 1) != 0;
+    const int dir = __ldcg(&nd.dir), axis = q.axis;
     if (tid == 0)
         sLeft = 0;
     int got = 0;
     for (int b = 0; b < nt; b += blockDim.x) {
         const int i = b + tid; // triangle index
         const int pos = i < nt ? posOf[i] : 0;
-        const int m = (i < nt && st_node(state[pos]) == id) ? 1 : 0;
+        const int m = (i < nt && st_node(__ldcg(&state[pos])) == id) ? 1 : 0;
         int tot;
         const int at = block_exclusive_scan(m, tot, warpSums);
         if (m && got + at < n)
             list[got + at] = pos;
         got += tot;
     }
-    const int dir = nd.dir, axis = q.axis;
+    __syncthreads();
     if (amb) {
         if (tid == 0) {
             double s = 0.0;
             for (int k = 0; k < n; ++k)
-                s = s + rec[list[dir ? n - 1 - k : k]].c[axis];
+                s = s + ord_to_dbl(rec[__ldcg(&list[dir ? n - 1 - k : k])].c[axis]);
             sSplit = s / (double)(float)n;
         }
         __syncthreads();
     }
     int myLeft = 0;
     for (int k = tid; k < n; k += blockDim.x) {
-        const double c = rec[list[k]].c[axis];
-        myLeft += (amb ? (c < sSplit) : (ordc(c) < q.clo)) ? 1 : 0;
+        const unsigned long long c = rec[__ldcg(&list[k])].c[axis];
+        myLeft += (amb ? (ord_to_dbl(c) < sSplit) : (c < q.clo)) ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1)
         myLeft += __shfl_xor_sync(0xFFFFFFFFu, myLeft, o);
@@ -622,12 +791,13 @@ __device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *
     for (int k0 = 0; k0 < n; k0 += blockDim.x) {
         const int k = k0 + tid;
         int sd = -1;
+        int pos = 0;
         if (k < n) {
-            const int pos = list[k];
+            pos = __ldcg(&list[k]);
             const int mp = dir ? n - 1 - k : k; // position in member order
             if (mode == 0) {
-                const double c = rec[pos].c[axis];
-                sd = (amb ? (c < sSplit) : (ordc(c) < q.clo)) ? 0 : 1;
+                const unsigned long long c = rec[pos].c[axis];
+                sd = (amb ? (ord_to_dbl(c) < sSplit) : (c < q.clo)) ? 0 : 1;
             } else if (mode == 1) {
                 sd = mp < n / 2 ? 0 : 1;               // all right, in member order: halves
             } else {
@@ -635,114 +805,117 @@ __device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *
             }
             state[pos] = (id << 2) | (sd + 1);
         }
-        const EStat e = estat_of(sd >= 0, rec[k < n ? list[k] : 0], sc);
+        const EStat e = estat_of(sd >= 0, rec[pos]);
         block_reduce_keys(sd, e, sd >= 0 ? 1 : 0, runs, warpSums, [&](int qq) -> RStat & { return sAcc[qq]; });
     }
+    __syncthreads();
     if (tid < 2)
         nd.acc[tid] = sAcc[tid];
-    if (tid == 0) {
+    if (tid == 0)
         nd.mode = mode;
-        nd.flags = 0;
-    }
+    __threadfence(); // state words and accumulators reach L2 before anyone reads them through it
     __syncthreads();
 }
 
-// One block per level: resolves the rare nodes that need their member order, allocates the children of every
-// node split at this level (block scans, no atomics), fills their statistics and split parameters, lists the
-// terminal ones, and advances the level bounds.
-__global__ void __launch_bounds__(kWide) k_rr_children(int nt, RNode *nodes, NParam *np, int *counters, int *terms,
-                                                       int maxNodes, const RRec *__restrict__ rec, int *state,
-                                                       const int *__restrict__ posOf, int *pool,
-                                                       const int *__restrict__ scg)
+// The children of one split node, one thread each (threads 0 and 1; all threads of the block call it): ids
+// and terminal-list slots from atomic counters (node ids carry no order; begin offsets and direction bits
+// do), statistics and split parameters.
+__device__ void create_children(int id, RNode *nodes, NParam *np, int *counters, int *terms, int maxNodes,
+                                const int *sc, int *sBase)
 {
-    __shared__ int warpSums[32];
+    RNode &nd = nodes[id];
+    if (threadIdx.x == 0) {
+        const int c = atomicAdd(counters + kCtNodes, 2);
+        if (c + 2 > maxNodes) {
+            atomicExch(counters + kCtOverflow, 1); // nothing is split further; the host reports the overflow
+            *sBase = -1;
+        } else {
+            *sBase = c;
+        }
+    }
+    __syncthreads();
+    const int c = *sBase;
+    const int s2 = threadIdx.x;
+    if (c >= 0 && s2 < 2) {
+        const RStat acc = ld_rstat(&nd.acc[s2]);
+        const int leftCount = __ldcg(&nd.acc[0].count);
+        const int mode = __ldcg(&nd.mode), dir = __ldcg(&nd.dir), begin = __ldcg(&nd.begin);
+        const int dl = mode == 1 ? dir : dir ^ 1;
+        const int dr = mode == 2 ? dir ^ 1 : dir;
+        RNode &ch = nodes[c + s2];
+        const int cnt = acc.count;
+        ch.begin = s2 == 0 ? begin : begin + leftCount;
+        ch.count = cnt;
+        ch.dir = s2 == 0 ? dl : dr;
+        ch.flags = 0;
+        ch.mode = 0;
+        ch.pad[0] = ch.pad[1] = ch.pad[2] = 0;
+        ch.st = acc;
+        rstat_clear(ch.acc[0]);
+        rstat_clear(ch.acc[1]);
+        NParam cq{-1, cnt, 0, 0, 0ull, 0ull};
+        if (cnt > kSub)
+            node_params(acc.lo, acc.hi, acc.sum, cnt, sc, cq.axis, cq.clo, cq.chi);
+        else
+            terms[atomicAdd(counters + kCtTerms, 1)] = c + s2;
+        np[c + s2] = cq;
+        if (s2 == 0)
+            np[id].child = c; // read only after the grid barrier that ends this phase
+    }
+    __syncthreads(); // sBase is reused by the next node of this block
+}
+
+__global__ void __launch_bounds__(kElemThreads, 4)
+    k_rr_top(int nt, const RRec *__restrict__ rec, const unsigned long long *__restrict__ soa, int *state, NParam *np,
+             RNode *nodes, int *counters, int *terms,
+             int maxNodes, const int *__restrict__ posOf, int *pool, const int *__restrict__ scg, GridBar *gb)
+{
     __shared__ RunRec runs[kRunCap];
+    __shared__ int warpRuns[32];
     __shared__ RStat sAcc[2];
-    __shared__ int sLeft, nFlag;
+    __shared__ int sLeft;
     __shared__ double sSplit;
-    __shared__ int flagged[kWide];
-    const int first = counters[kCtFirst], last = counters[kCtLast];
-    if (first >= last)
-        return;
-    const int tid = threadIdx.x;
     const int sc[3] = {scg[0], scg[1], scg[2]};
-    // nodes that need the exact, order-aware resolution
-    for (int b = first; b < last; b += kWide) {
-        if (tid == 0)
-            nFlag = 0;
-        __syncthreads();
-        const int id = b + tid;
-        if (id < last) {
-            const RNode &nd = nodes[id];
-            if (nd.count > kSub && ((nd.flags & 1) || nd.acc[0].count == 0 || nd.acc[1].count == 0))
-                flagged[atomicAdd(&nFlag, 1)] = id;
+    __shared__ LevelTab tab;
+    int first = __ldcg(&counters[kCtFirst]), last = __ldcg(&counters[kCtLast]), prevFirst = first;
+    for (int level = 0; level < kMaxLevels && first < last; ++level) {
+        load_level_tab(tab, np, prevFirst, first, last);
+        {
+            // contiguous Morton ranges: block slices of whole chunks, split among the block's warps
+            const int warps = blockDim.x >> 5, w = threadIdx.x >> 5;
+            const int chunks = (nt + 31) >> 5;
+            const int perBlock = (chunks + gridDim.x - 1) / gridDim.x;
+            const int perWarp = (perBlock + warps - 1) / warps;
+            const int c0 = min(chunks, (int)blockIdx.x * perBlock + w * perWarp);
+            const int c1 = min(min(chunks, ((int)blockIdx.x + 1) * perBlock), c0 + perWarp);
+            classify_range(32 * c0, min(nt, 32 * c1), prevFirst, first, last, soa, nt, state, np, nodes, runs,
+                           warpRuns, tab);
         }
-        __syncthreads();
-        const int nf = nFlag;
-        for (int f = 0; f < nf; ++f) {
-            const int fid = flagged[f];
-            const NParam q = np[fid];
-            resolve_node(fid, nt, rec, state, q, nodes[fid], pool, posOf, sc, warpSums, runs, sAcc, sLeft, sSplit);
+        if (!grid_sync(gb))
+            return;
+        for (int id = first + blockIdx.x; id < last; id += gridDim.x) {
+            RNode &nd = nodes[id];
+            const int count = __ldcg(&nd.count);
+            if (count <= kSub)
+                continue;
+            const bool flagged = (__ldcg(&nd.flags) & 1) || __ldcg(&nd.acc[0].count) == 0 ||
+                                 __ldcg(&nd.acc[1].count) == 0;
+            if (flagged) // members of one level's nodes are disjoint: the node's leaf range is its list space
+                resolve_node(id, nt, rec, state, ld_nparam(&np[id]), nd, pool + __ldcg(&nd.begin), posOf, warpRuns,
+                             runs, sAcc, sLeft, sSplit);
+            create_children(id, nodes, np, counters, terms, maxNodes, sc, &sLeft);
         }
-        __syncthreads();
+        if (!grid_sync(gb))
+            return;
+        prevFirst = first;
+        first = last;
+        last = min(__ldcg(&counters[kCtNodes]), maxNodes);
+        if (__ldcg(&counters[kCtOverflow]))
+            break;
     }
-    // children
-    int nodeBase = counters[kCtNodes], termBase = counters[kCtTerms];
-    bool overflow = false;
-    for (int b = first; b < last; b += kWide) {
-        const int id = b + tid;
-        const RNode *nd = id < last ? &nodes[id] : nullptr;
-        const int split = (nd && nd->count > kSub) ? 1 : 0;
-        int totSplit;
-        const int at = block_exclusive_scan(split, totSplit, warpSums);
-        const int c = nodeBase + 2 * at;
-        const bool ok = split && c + 2 <= maxNodes;
-        overflow |= split && !ok;
-        int nTerm = 0, cnt[2] = {0, 0};
-        if (ok) {
-            const int mode = nd->mode, dir = nd->dir;
-            const int dl = mode == 1 ? dir : dir ^ 1;
-            const int dr = mode == 2 ? dir ^ 1 : dir;
-            for (int s2 = 0; s2 < 2; ++s2) {
-                cnt[s2] = nd->acc[s2].count;
-                RNode &ch = nodes[c + s2];
-                ch.begin = s2 == 0 ? nd->begin : nd->begin + nd->acc[0].count;
-                ch.count = cnt[s2];
-                ch.dir = s2 == 0 ? dl : dr;
-                ch.flags = 0;
-                ch.mode = 0;
-                ch.pad[0] = ch.pad[1] = ch.pad[2] = 0;
-                ch.st = nd->acc[s2];
-                rstat_clear(ch.acc[0]);
-                rstat_clear(ch.acc[1]);
-                NParam cq{-1, cnt[s2], 0, 0, 0ull, 0ull};
-                if (cnt[s2] > kSub)
-                    node_params(ch.st.lo, ch.st.hi, ch.st.sum, cnt[s2], sc, cq.axis, cq.clo, cq.chi);
-                else
-                    ++nTerm;
-                np[c + s2] = cq;
-            }
-            np[id].child = c;
-        }
-        int totTerm;
-        const int tat = block_exclusive_scan(nTerm, totTerm, warpSums);
-        if (ok) {
-            int t2 = termBase + tat;
-            for (int s2 = 0; s2 < 2; ++s2)
-                if (cnt[s2] <= kSub)
-                    terms[t2++] = c + s2;
-        }
-        nodeBase += 2 * totSplit;
-        termBase += totTerm;
-    }
-    overflow = __syncthreads_or(overflow);
-    if (tid == 0) {
-        counters[kCtNodes] = nodeBase < maxNodes ? nodeBase : maxNodes;
-        counters[kCtTerms] = termBase;
-        if (overflow)
-            counters[kCtOverflow] = 1;
-        counters[kCtFirst] = last;
-        counters[kCtLast] = overflow ? last : counters[kCtNodes];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counters[kCtFirst] = first;
+        counters[kCtLast] = last;
     }
 }
 
@@ -794,7 +967,7 @@ __device__ __forceinline__ void snode_init(SNode &n, int begin, int count)
 // about 55 KB: four blocks per SM
 constexpr size_t kSubSmem = sizeof(SNode) * kSubNodes + sizeof(int) * (6 * kSub + 1 + kSubThreads / 32);
 
-__global__ void __launch_bounds__(kSubThreads)
+__global__ void __launch_bounds__(kSubThreads, 4)
     k_rr_subtree(const int *__restrict__ terms, const RNode *__restrict__ gnodes, const int *__restrict__ sorted,
                  const RRec *__restrict__ rec, const int *__restrict__ posOf, const int *__restrict__ leafTri,
                  const int *__restrict__ scg, int *rank, int *counters)
@@ -808,6 +981,8 @@ __global__ void __launch_bounds__(kSubThreads)
     int *warpSum = scan + kSub + 1;
     __shared__ int nNodes, lFirst, lLast, anyAmb, err;
     const int tid = threadIdx.x;
+    if ((int)blockIdx.x >= counters[kCtTerms])
+        return;
     const RNode &g = gnodes[terms[blockIdx.x]];
     const int base = g.begin, n = g.count, dir = g.dir;
     int sc[3] = {scg[0], scg[1], scg[2]};
@@ -861,7 +1036,7 @@ __global__ void __launch_bounds__(kSubThreads)
             if (id >= first) {
                 SNode &nd = nodes[id];
                 if (nd.count > kLeaf) {
-                    const unsigned long long o = ordc(rec[perm[cur][p]].c[nd.axis]);
+                    const unsigned long long o = rec[perm[cur][p]].c[nd.axis];
                     if (o < nd.clo)
                         f = 1;
                     else if (o < nd.chi) {
@@ -881,10 +1056,10 @@ __global__ void __launch_bounds__(kSubThreads)
                     continue;
                 double s = 0.0;
                 for (int p = nd.begin; p < nd.begin + nd.count; ++p)
-                    s = s + rec[perm[cur][p]].c[nd.axis];
+                    s = s + ord_to_dbl(rec[perm[cur][p]].c[nd.axis]);
                 const double split = s / (double)(float)nd.count;
                 for (int p = nd.begin; p < nd.begin + nd.count; ++p)
-                    flag[p] = rec[perm[cur][p]].c[nd.axis] < split ? 1 : 0;
+                    flag[p] = ord_to_dbl(rec[perm[cur][p]].c[nd.axis]) < split ? 1 : 0;
             }
             __syncthreads();
         }
@@ -966,42 +1141,85 @@ __global__ void __launch_bounds__(kSubThreads)
             nodeOf[cur ^ 1][q] = nodes[ch].count > kLeaf ? ch : -2; // leaves need no statistics
         }
         __syncthreads();
-        // Statistics of the children that split again, read in the new order. A node's members are
-        // contiguous, so each warp's runs end either at a node's last member (that run's total goes to the
-        // node) or at the warp's last lane (kept per 32-position chunk); one thread per node then adds the
-        // chunk totals inside its range. No atomics.
-        EStat *chunk = reinterpret_cast<EStat *>(scan); // the scan is consumed; kSub / 32 entries fit
-        for (int p0 = 0; p0 < n; p0 += kSubThreads) {
-            const int p = p0 + tid;
-            const int id = p < n ? nodeOf[cur ^ 1][p] : -1;
-            const int key = id >= 0 ? id : -1;
-            EStat e = estat_of(key >= 0, rec[key >= 0 ? perm[cur ^ 1][p] : 0], sc);
-            int len = 1;
-            if (warp_segment_reduce(key, e, len) && key >= 0) {
-                SNode &nd = nodes[key];
-                if (p == nd.begin + nd.count - 1) {
-                    for (int k = 0; k < 3; ++k) {
-                        nd.lo[k] = e.lo[k];
-                        nd.hi[k] = e.hi[k];
-                        nd.sum[k] = e.s[k];
+        // Statistics of the children that split again, read in the new order. A node's members are contiguous
+        // and number more than 20, so the kPer consecutive positions of one thread hold at most a head run
+        // that ends a node inside the thread and a tail run that continues past it (a run in between can only
+        // be of settled members). A segmented scan over the threads' tail runs gives each run's total where it
+        // ends: a node's total is written to the node, a run cut at a warp's last position is kept per chunk,
+        // and one thread per node then adds the chunk totals inside its range. No atomics.
+        {
+            constexpr int kPer = kSub / kSubThreads;
+            constexpr int kChunk = 32 * kPer; // positions per warp
+            EStat *chunk = reinterpret_cast<EStat *>(scan); // the scan is consumed; kSubThreads / 32 entries fit
+            const int lane = tid & 31, w = tid >> 5;
+            const int lastPos = kPer * tid + kPer - 1;
+            int kHead = -1, kTail = -1;
+            bool split = false;
+            EStat head, tail;
+            estat_neutral(head);
+            estat_neutral(tail);
+            for (int j = 0; j < kPer; ++j) {
+                const int p = kPer * tid + j;
+                const int id = p < n ? nodeOf[cur ^ 1][p] : -1;
+                const int key = id >= 0 ? id : -1;
+                if (j == 0) {
+                    kTail = key;
+                } else if (key != kTail) {
+                    if (!split) {
+                        kHead = kTail;
+                        head = tail;
+                        split = true;
                     }
-                } else {
-                    chunk[p >> 5] = e; // p is the last position of its chunk
+                    kTail = key;
+                    estat_neutral(tail);
+                }
+                if (key >= 0)
+                    estat_merge(tail, estat_of(true, rec[perm[cur ^ 1][p]]));
+            }
+            const int prevKey = __shfl_up_sync(0xFFFFFFFFu, kTail, 1);
+            EStat run = tail;
+            warp_segmented_scan(lane == 0 || split || prevKey != kTail, run);
+            EStat prev;
+            for (int k = 0; k < 3; ++k) {
+                prev.lo[k] = __shfl_up_sync(0xFFFFFFFFu, run.lo[k], 1);
+                prev.hi[k] = __shfl_up_sync(0xFFFFFFFFu, run.hi[k], 1);
+                prev.s[k] = __shfl_up_sync(0xFFFFFFFFu, run.s[k], 1);
+            }
+            if (split && kHead >= 0) {
+                if (lane > 0 && prevKey == kHead)
+                    estat_merge(head, prev);
+                SNode &nd = nodes[kHead];
+                for (int k = 0; k < 3; ++k) {
+                    nd.lo[k] = head.lo[k];
+                    nd.hi[k] = head.hi[k];
+                    nd.sum[k] = head.s[k];
                 }
             }
-        }
-        __syncthreads();
-        for (int id = last + tid; id < nNodes; id += kSubThreads) {
-            SNode &nd = nodes[id];
-            if (nd.count <= kLeaf)
-                continue;
-            const int b = nd.begin, e = nd.begin + nd.count - 1; // chunk ends in [b, e) belong to the node
-            for (int j = b >> 5; 32 * j + 31 < e; ++j) { // 32 (b / 32) + 31 is the first chunk end >= b
-                const EStat &c = chunk[j];
-                for (int k = 0; k < 3; ++k) {
-                    nd.lo[k] = min(nd.lo[k], c.lo[k]);
-                    nd.hi[k] = max(nd.hi[k], c.hi[k]);
-                    nd.sum[k] += c.s[k];
+            if (kTail >= 0) {
+                SNode &nd = nodes[kTail];
+                if (nd.begin + nd.count - 1 == lastPos) {
+                    for (int k = 0; k < 3; ++k) {
+                        nd.lo[k] = run.lo[k];
+                        nd.hi[k] = run.hi[k];
+                        nd.sum[k] = run.s[k];
+                    }
+                } else if (lane == 31) {
+                    chunk[w] = run;
+                }
+            }
+            __syncthreads();
+            for (int id = last + tid; id < nNodes; id += kSubThreads) {
+                SNode &nd = nodes[id];
+                if (nd.count <= kLeaf)
+                    continue;
+                const int b = nd.begin, e = nd.begin + nd.count - 1; // chunk ends in [b, e) belong to the node
+                for (int j = b / kChunk; kChunk * j + kChunk - 1 < e; ++j) {
+                    const EStat &c = chunk[j];
+                    for (int k = 0; k < 3; ++k) {
+                        nd.lo[k] = min(nd.lo[k], c.lo[k]);
+                        nd.hi[k] = max(nd.hi[k], c.hi[k]);
+                        nd.sum[k] += c.s[k];
+                    }
                 }
             }
         }
@@ -1029,6 +1247,34 @@ static int bit_length(int x)
     return b;
 }
 
+// Blocks of the cooperative large-node kernel: half of what can be resident at once (the two meshes of a
+// boolean are prepared concurrently, so two such grids must fit together), no more than the members need.
+// Cached per device.
+static int top_grid(int nt)
+{
+    static int perSm[256], sms[256];
+    static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
+        return -1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (perSm[dev] == 0) {
+            int coop = 0;
+            if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+                cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm[dev], k_rr_top, kElemThreads, 0) != cudaSuccess ||
+                perSm[dev] <= 0) {
+                set_last_error("cooperative launch unavailable for the reference tree build");
+                perSm[dev] = 0;
+                return -1;
+            }
+        }
+    }
+    const int need = (nt + kElemThreads * 4 - 1) / (kElemThreads * 4); // at least 4 members per thread
+    return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 2)));
+}
+
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
 {
     MeshDev &d = m->d;
@@ -1044,64 +1290,66 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, (int *)nullptr, (int *)nullptr, (int *)nullptr,
                                     (int *)nullptr, nt, 0, keyBits, s);
     Carve c;
-    const size_t o_rec = c.take<RRec>(nt), o_state = c.take<int>(nt), o_pos = c.take<int>(nt);
+    const size_t o_rec = c.take<RRec>(nt), o_soa = c.take<unsigned long long>((size_t)12 * nt),
+                 o_state = c.take<int>(nt), o_pos = c.take<int>(nt);
     const size_t o_key = c.take<int>(nt), o_val = c.take<int>(nt), o_skey = c.take<int>(nt),
                  o_sval = c.take<int>(nt), o_pool = c.take<int>(nt);
     const size_t o_np = c.take<NParam>(maxNodes);
     const size_t o_nodes = c.take<RNode>(maxNodes), o_terms = c.take<int>(maxNodes), o_ct = c.take<int>(kCtCount),
-                 o_sc = c.take<int>(4), o_cub = c.take<char>(sortBytes);
+                 o_sc = c.take<int>(4), o_bar = c.take<GridBar>(1), o_cub = c.take<char>(sortBytes);
     SB_CUDA_CHECK(m->tmp.ensure(c.off));
     char *b = m->tmp.as<char>();
     RRec *rec = (RRec *)(b + o_rec);
+    unsigned long long *soa = (unsigned long long *)(b + o_soa);
     int *state = (int *)(b + o_state);
     NParam *np = (NParam *)(b + o_np);
     int *key = (int *)(b + o_key), *val = (int *)(b + o_val), *skey = (int *)(b + o_skey), *sval = (int *)(b + o_sval);
     int *pool = (int *)(b + o_pool), *posOf = (int *)(b + o_pos);
     RNode *nodes = (RNode *)(b + o_nodes);
     int *terms = (int *)(b + o_terms), *counters = (int *)(b + o_ct), *scg = (int *)(b + o_sc);
+    GridBar *bar = (GridBar *)(b + o_bar);
 
     const int GE = (nt + kElemThreads - 1) / kElemThreads;
-    SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters);
-    SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, posOf, state, nodes);
-    SB_COUNT(k_rr_root_sum)<<<GE, kElemThreads, 0, s>>>(nt, rec, nodes, scg);
+    SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters, reinterpret_cast<unsigned *>(bar));
+    SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, soa, posOf, state,
+                                                      nodes);
+    SB_COUNT(k_rr_root_sum)<<<GE, kElemThreads, 0, s>>>(nt, rec, soa, nodes, scg);
     SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, np, nt, scg, counters, terms);
-    // levels run in batches; the host looks at the level bounds only between batches. The first batch
-    // covers the expected depth of the large-node phase (a mean split roughly halves); empty levels cost
-    // only their launches.
-    int expected = 0;
-    while ((nt >> expected) > kSub)
-        ++expected;
-    bool done = nt <= kSub;
-    int cnt[kCtCount] = {0};
-    for (int level = 0, batch = expected + 1; level < 4096 && !done; level += batch, batch = 2) {
-        for (int j = 0; j < batch; ++j) {
-            SB_COUNT(k_rr_classify)<<<GE, kElemThreads, 0, s>>>(nt, counters, rec, state, np, nodes, scg);
-            SB_COUNT(k_rr_children)<<<1, kWide, 0, s>>>(nt, nodes, np, counters, terms, maxNodes, rec, state, posOf,
-                                                        pool, scg);
-        }
-        SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaStreamSynchronize(s));
-        if (cnt[kCtOverflow] != 0) {
-            set_last_error("reference tree node capacity exceeded");
-            return SB_ERR_CAPACITY;
-        }
-        done = cnt[kCtFirst] >= cnt[kCtLast];
+    // the large-node phase: one cooperative launch, every block resident
+    if (nt > kSub) {
+        const int topBlocks = top_grid(nt);
+        if (topBlocks <= 0)
+            return SB_ERR_CUDA;
+        void *args[] = {(void *)&nt, (void *)&rec, (void *)&soa, (void *)&state, (void *)&np, (void *)&nodes, (void *)&counters,
+                        (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar};
+        count_launch();
+        SB_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)k_rr_top, dim3(topBlocks), dim3(kElemThreads), args, 0, s));
     }
-    if (!done) {
-        set_last_error("reference tree deeper than 4096 levels");
-        return SB_ERR_CAPACITY;
-    }
-    if (nt <= kSub)
-        cnt[kCtTerms] = 1;
     SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
     SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem));
-    SB_COUNT(k_rr_subtree)<<<cnt[kCtTerms], kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri, scg, d.rank,
-                                                                        counters);
-    int errs = 0;
-    SB_CUDA_CHECK(cudaMemcpyAsync(&errs, counters + kCtSubErr, sizeof errs, cudaMemcpyDeviceToHost, s));
+    // one block per terminal node; the count is known only on the device, so the grid covers every node record
+    // that could be terminal and the surplus blocks return at once
+    SB_COUNT(k_rr_subtree)<<<maxNodes, kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri, scg,
+                                                                    d.rank, counters);
+    int cnt[kCtCount];
+    GridBar hb;
+    SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(&hb, bar, sizeof hb, cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
-    if (errs) {
+    if (hb.err) {
+        set_last_error("reference tree: a grid barrier timed out");
+        return SB_ERR_CUDA;
+    }
+    if (cnt[kCtOverflow]) {
+        set_last_error("reference tree node capacity exceeded");
+        return SB_ERR_CAPACITY;
+    }
+    if (cnt[kCtFirst] < cnt[kCtLast]) {
+        set_last_error("reference tree deeper than the level limit");
+        return SB_ERR_CAPACITY;
+    }
+    if (cnt[kCtSubErr]) {
         set_last_error("reference tree: a subtree exceeded its node records");
         return SB_ERR_CAPACITY;
     }
