@@ -187,6 +187,99 @@ __global__ void k_hi32(int n, const uint64_t *__restrict__ k, int *out)
         out[i] = (int)(k[i] >> 32);
 }
 
+// Groups the intersecting pairs by cut face when one side's pairs fit one block: a block radix sort of the
+// compacted keys (face << orderBits | order, the order being the other triangle's leaf position), then the
+// runs of equal face (unique faces, their pair counts and how many there are), in one launch. Block 0 takes
+// the first mesh's faces, block 1 the second's; the pair indices land in pairIdx[side * K + i].
+constexpr int kGroupThreads = 512;
+constexpr int kGroupItems = 16;
+constexpr int kGroupMax = kGroupThreads * kGroupItems;
+using GroupSort = cub::BlockRadixSort<unsigned long long, kGroupThreads, kGroupItems, int>;
+union GroupSmem {
+    typename GroupSort::TempStorage sort;
+    int starts[kGroupMax + 1];
+};
+
+__global__ void __launch_bounds__(kGroupThreads)
+    k_face_group(int K, const uint64_t *__restrict__ keyA, const uint64_t *__restrict__ keyB,
+                 const int *__restrict__ val, int orderBitsA, int orderBitsB, int endBitA, int endBitB,
+                 int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB, unsigned int *runCount)
+{
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    GroupSmem &sm = *reinterpret_cast<GroupSmem *>(smemRaw);
+    __shared__ int warpSums[kGroupThreads / 32];
+    const int side = blockIdx.x;
+    const uint64_t *keys = side ? keyB : keyA;
+    const int ob = side ? orderBitsB : orderBitsA, endBit = side ? endBitB : endBitA;
+    int *uq = side ? uqB : uqA, *ct = side ? ctB : ctA;
+    unsigned long long k[kGroupItems];
+    int v[kGroupItems];
+    const unsigned long long pad = endBit >= 64 ? ~0ull : ((1ull << endBit) - 1);
+    for (int j = 0; j < kGroupItems; ++j) {
+        const int i = threadIdx.x * kGroupItems + j;
+        if (i < K) {
+            const uint64_t key = keys[i];
+            k[j] = ((key >> 32) << ob) | (key & 0xFFFFFFFFull);
+            v[j] = val[i];
+        } else {
+            k[j] = pad; // sorts after every real key (LSD radix sort is stable and these come last)
+            v[j] = -1;
+        }
+    }
+    GroupSort(sm.sort).Sort(k, v, 0, endBit);
+    __syncthreads(); // the sort storage is reused below
+    int flags = 0;
+    int prevFace = -1;
+    const int i0 = threadIdx.x * kGroupItems;
+    __shared__ int lastFace[kGroupThreads]; // face of each thread's last item, for its successor
+    lastFace[threadIdx.x] = (int)(k[kGroupItems - 1] >> ob);
+    __syncthreads();
+    prevFace = threadIdx.x > 0 ? lastFace[threadIdx.x - 1] : -1;
+    for (int j = 0; j < kGroupItems; ++j) {
+        const int i = i0 + j;
+        const int face = (int)(k[j] >> ob);
+        if (i < K) {
+            pairIdx[(size_t)side * K + i] = v[j];
+            flags += (i == 0 || face != prevFace) ? 1 : 0;
+        }
+        prevFace = face;
+    }
+    // run index of each face start
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = flags;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o)
+            incl += t;
+    }
+    if (lane == 31)
+        warpSums[w] = incl;
+    __syncthreads();
+    int run = incl - flags, total = 0;
+    for (int q = 0; q < kGroupThreads / 32; ++q) {
+        run += q < w ? warpSums[q] : 0;
+        total += warpSums[q];
+    }
+    prevFace = threadIdx.x > 0 ? lastFace[threadIdx.x - 1] : -1;
+    for (int j = 0; j < kGroupItems; ++j) {
+        const int i = i0 + j;
+        const int face = (int)(k[j] >> ob);
+        if (i < K && (i == 0 || face != prevFace)) {
+            uq[run] = face;
+            sm.starts[run] = i;
+            ++run;
+        }
+        prevFace = face;
+    }
+    if (threadIdx.x == 0)
+        sm.starts[total] = K;
+    __syncthreads();
+    for (int r = threadIdx.x; r < total; r += kGroupThreads)
+        ct[r] = sm.starts[r + 1] - sm.starts[r];
+    if (threadIdx.x == 0)
+        runCount[side] = (unsigned int)total;
+}
+
 __global__ void k_face_table(int FA, int FB, const int *__restrict__ uniqA, const int *__restrict__ cntA,
                              const int *__restrict__ uniqB, const int *__restrict__ cntB, int *faceSide,
                              int *faceTri, int *faceCnt)
@@ -296,8 +389,6 @@ template <class F> sb_status guarded(F &&f)
     }
 }
 
-size_t cub_need = 0;
-
 // CUB wrappers: query, grow the handle's temp buffer, run
 template <class Call> cudaError_t cub_run(sb_boolean *b, Call &&call)
 {
@@ -392,18 +483,17 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_seg = cc.take<double>((size_t)b->candCap * 6);
     size_t o_sel = cc.take<int>(b->candCap);
     uint64_t *candRaw = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw);
-    uint64_t *candSorted = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_srt);
+    uint64_t *candSorted = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_srt); // unused, see below
     uint8_t *hit = reinterpret_cast<uint8_t *>(b->cand.as<char>() + o_hit);
     double *seg = reinterpret_cast<double *>(b->cand.as<char>() + o_seg);
     int *sel = reinterpret_cast<int *>(b->cand.as<char>() + o_sel);
+    // Candidates stay in emission order: every later ordering is by unique keys (face, the other triangle's
+    // leaf position), so the result does not depend on it.
+    (void)candSorted;
+    candSorted = candRaw;
     b->C = (int)C;
     b->d_cand = candSorted;
     st.candidate_pairs = C;
-    const int endBit = end_bit_for((uint64_t)std::max(nA, 1) * (uint64_t)std::max(nB, 1));
-    if (C > 0)
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRadixSort::SortKeys(tmp, bytes, candRaw, candSorted, (int)C, 0, endBit, s);
-        }));
     SB_CUDA_CHECK(cudaEventRecord(b->ev[1], s));
 
     // ---------------- narrow phase ----------------
@@ -449,20 +539,31 @@ sb_status combine_impl(sb_boolean *b)
     if (K > 0) {
         SB_COUNT(k_pair_keys)<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
                                                    useRank ? B.rank : nullptr, seg, keyA, keyB, val, segK, pairAB);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
-        }));
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K, 0, 64, s);
-        }));
-        SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
-        SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiA, uqA, ctA, d_count + 2, (int)K, s);
-        }));
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiB, uqB, ctB, d_count + 3, (int)K, s);
-        }));
+        if (K <= (unsigned int)kGroupMax) {
+            const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
+            const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
+            static std::once_flag smemOnce;
+            std::call_once(smemOnce, [] {
+                cudaFuncSetAttribute(k_face_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupSmem));
+            });
+            SB_COUNT(k_face_group)<<<2, kGroupThreads, sizeof(GroupSmem), s>>>(
+                (int)K, keyA, keyB, val, obA, obB, ebA, ebB, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
+        } else {
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
+            }));
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K, 0, 64, s);
+            }));
+            SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
+            SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiA, uqA, ctA, d_count + 2, (int)K, s);
+            }));
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiB, uqB, ctB, d_count + 3, (int)K, s);
+            }));
+        }
         unsigned int runs[2];
         sb_status r = read_back(b, runs, d_count + 2, sizeof runs);
         if (r != SB_OK)
