@@ -191,39 +191,31 @@ template <bool FP64> struct TriTri {
         return ps(base) - sv;
     }
 
-    // CONSTRUCT_INTERSECTION (tri_tri_intersect.c:285-356) on slots already in canonical order
-    __device__ int construct(int p1, int q1, int r1, int p2, int q2, int r2, double *out)
+    // CONSTRUCT_INTERSECTION (tri_tri_intersect.c:285-356) on slots already in canonical order. The four
+    // outcomes differ only in which vertices and which normal the two end points use, so they are chosen as
+    // data and computed once (one copy of the code keeps the kernel small).
+    __device__ int construct(const int *v, double *out)
     {
-        int t1 = orient(p2, p1, q1, p1, r2, p1);
+        const int p1 = v[0], q1 = v[1], r1 = v[2], p2 = v[3], q2 = v[4], r2 = v[5];
         int which; // 0: (p1 r1 N2, p2 r2 N1)  1: (p2 q2 N1, p2 r2 N1)  2: (p1 r1 N2, p1 q1 N2)  3: (p2 q2 N1, p1 q1 N2)
-        if (t1 > 0) {
-            if (orient(p2, p1, r1, p1, r2, p1) <= 0) {
-                which = orient(p2, p1, r1, p1, q2, p1) > 0 ? 0 : 1;
-            } else {
+        if (orient(p2, p1, q1, p1, r2, p1) > 0) {
+            if (orient(p2, p1, r1, p1, r2, p1) > 0)
                 return 0;
-            }
+            which = orient(p2, p1, r1, p1, q2, p1) > 0 ? 0 : 1;
         } else {
             if (orient(p2, p1, q1, p1, q2, p1) < 0)
                 return 0;
             which = orient(p2, p1, r1, p1, q2, p1) >= 0 ? 2 : 3;
         }
         load64();
-        d3 N1 = cross(ps(1) - ps(0), ps(2) - ps(0));
-        d3 N2 = cross(ps(3) - ps(5), ps(4) - ps(5));
-        d3 s, t;
-        if (which == 0) {
-            s = along(p1, p2, r1, N2);
-            t = along(p2, p1, r2, N1);
-        } else if (which == 1) {
-            s = along(p2, p1, q2, N1);
-            t = along(p2, p1, r2, N1);
-        } else if (which == 2) {
-            s = along(p1, p2, r1, N2);
-            t = along(p1, p2, q1, N2);
-        } else {
-            s = along(p2, p1, q2, N1);
-            t = along(p1, p2, q1, N2);
-        }
+        const d3 N1 = cross(ps(1) - ps(0), ps(2) - ps(0));
+        const d3 N2 = cross(ps(3) - ps(5), ps(4) - ps(5));
+        // first end point: which 0, 2 -> along(p1, p2, r1, N2); 1, 3 -> along(p2, p1, q2, N1)
+        const bool sOn1 = which == 0 || which == 2;
+        const d3 s = along(sOn1 ? p1 : p2, sOn1 ? p2 : p1, sOn1 ? r1 : q2, sOn1 ? N2 : N1);
+        // second end point: which 0, 1 -> along(p2, p1, r2, N1); 2, 3 -> along(p1, p2, q1, N2)
+        const bool tOn2 = which <= 1;
+        const d3 t = along(tOn2 ? p2 : p1, tOn2 ? p1 : p2, tOn2 ? r2 : q1, tOn2 ? N1 : N2);
         out[0] = s.x;
         out[1] = s.y;
         out[2] = s.z;
@@ -233,38 +225,67 @@ template <bool FP64> struct TriTri {
         return 1;
     }
 
-    // TRI_TRI_INTER_3D (tri_tri_intersect.c:360-385); -1 = coplanar
-    __device__ int second(int p1, int q1, int r1, int p2, int q2, int r2, int dp2, int dq2, int dr2, double *out)
+    // TRI_TRI_INTER_3D (tri_tri_intersect.c:360-385): the slot order handed to CONSTRUCT_INTERSECTION, or
+    // false for the coplanar case
+    __device__ __forceinline__ static bool second(int p1, int q1, int r1, int p2, int q2, int r2, int dp2, int dq2,
+                                                  int dr2, int *v)
     {
+        // tri 1 either as given (p1 q1 r1) or swapped (p1 r1 q1); tri 2 in one of three rotations
+        int t1 = 0, rot = 0; // t1: 0 keep, 1 swap q1/r1; rot: 0 (p2 q2 r2), 1 (r2 p2 q2), 2 (q2 r2 p2)
         if (dp2 > 0) {
-            if (dq2 > 0)
-                return construct(p1, r1, q1, r2, p2, q2, out);
-            if (dr2 > 0)
-                return construct(p1, r1, q1, q2, r2, p2, out);
-            return construct(p1, q1, r1, p2, q2, r2, out);
+            if (dq2 > 0) {
+                t1 = 1;
+                rot = 1;
+            } else if (dr2 > 0) {
+                t1 = 1;
+                rot = 2;
+            } else {
+                t1 = 0;
+                rot = 0;
+            }
+        } else if (dp2 < 0) {
+            if (dq2 < 0) {
+                t1 = 0;
+                rot = 1;
+            } else if (dr2 < 0) {
+                t1 = 0;
+                rot = 2;
+            } else {
+                t1 = 1;
+                rot = 0;
+            }
+        } else if (dq2 < 0) {
+            if (dr2 >= 0) {
+                t1 = 1;
+                rot = 2;
+            } else {
+                t1 = 0;
+                rot = 0;
+            }
+        } else if (dq2 > 0) {
+            if (dr2 > 0) {
+                t1 = 1;
+                rot = 0;
+            } else {
+                t1 = 0;
+                rot = 2;
+            }
+        } else if (dr2 > 0) {
+            t1 = 0;
+            rot = 1;
+        } else if (dr2 < 0) {
+            t1 = 1;
+            rot = 1;
+        } else {
+            return false;
         }
-        if (dp2 < 0) {
-            if (dq2 < 0)
-                return construct(p1, q1, r1, r2, p2, q2, out);
-            if (dr2 < 0)
-                return construct(p1, q1, r1, q2, r2, p2, out);
-            return construct(p1, r1, q1, p2, q2, r2, out);
-        }
-        if (dq2 < 0) {
-            if (dr2 >= 0)
-                return construct(p1, r1, q1, q2, r2, p2, out);
-            return construct(p1, q1, r1, p2, q2, r2, out);
-        }
-        if (dq2 > 0) {
-            if (dr2 > 0)
-                return construct(p1, r1, q1, p2, q2, r2, out);
-            return construct(p1, q1, r1, q2, r2, p2, out);
-        }
-        if (dr2 > 0)
-            return construct(p1, q1, r1, r2, p2, q2, out);
-        if (dr2 < 0)
-            return construct(p1, r1, q1, r2, p2, q2, out);
-        return -1;
+        v[0] = p1;
+        v[1] = t1 ? r1 : q1;
+        v[2] = t1 ? q1 : r1;
+        v[3] = rot == 0 ? p2 : (rot == 1 ? r2 : q2);
+        v[4] = rot == 0 ? q2 : (rot == 1 ? p2 : r2);
+        v[5] = rot == 0 ? r2 : (rot == 1 ? q2 : p2);
+        return true;
     }
 
     // tri_tri_intersection_test_3d (tri_tri_intersect.c:395-472): 1 segment, 0 none, -1 coplanar
@@ -283,35 +304,62 @@ template <bool FP64> struct TriTri {
             return 0;
         const int dp1 = s1[0], dq1 = s1[1], dr1 = s1[2];
         const int dp2 = s2[0], dq2 = s2[1], dr2 = s2[2];
+        // tri 1 rotated to (r1 p1 q1), (q1 r1 p1) or kept; tri 2 kept or swapped (p2 r2 q2) with its signs
+        int rot1 = 0, sw2 = 0; // rot1: 0 (p1 q1 r1), 1 (r1 p1 q1), 2 (q1 r1 p1); sw2: 1 swaps q2/r2
         if (dp1 > 0) {
-            if (dq1 > 0)
-                return second(r1, p1, q1, p2, r2, q2, dp2, dr2, dq2, out);
-            if (dr1 > 0)
-                return second(q1, r1, p1, p2, r2, q2, dp2, dr2, dq2, out);
-            return second(p1, q1, r1, p2, q2, r2, dp2, dq2, dr2, out);
+            if (dq1 > 0) {
+                rot1 = 1;
+                sw2 = 1;
+            } else if (dr1 > 0) {
+                rot1 = 2;
+                sw2 = 1;
+            } else {
+                rot1 = 0;
+                sw2 = 0;
+            }
+        } else if (dp1 < 0) {
+            if (dq1 < 0) {
+                rot1 = 1;
+                sw2 = 0;
+            } else if (dr1 < 0) {
+                rot1 = 2;
+                sw2 = 0;
+            } else {
+                rot1 = 0;
+                sw2 = 1;
+            }
+        } else if (dq1 < 0) {
+            if (dr1 >= 0) {
+                rot1 = 2;
+                sw2 = 1;
+            } else {
+                rot1 = 0;
+                sw2 = 0;
+            }
+        } else if (dq1 > 0) {
+            if (dr1 > 0) {
+                rot1 = 0;
+                sw2 = 1;
+            } else {
+                rot1 = 2;
+                sw2 = 0;
+            }
+        } else if (dr1 > 0) {
+            rot1 = 1;
+            sw2 = 0;
+        } else if (dr1 < 0) {
+            rot1 = 1;
+            sw2 = 1;
+        } else {
+            return -1;
         }
-        if (dp1 < 0) {
-            if (dq1 < 0)
-                return second(r1, p1, q1, p2, q2, r2, dp2, dq2, dr2, out);
-            if (dr1 < 0)
-                return second(q1, r1, p1, p2, q2, r2, dp2, dq2, dr2, out);
-            return second(p1, q1, r1, p2, r2, q2, dp2, dr2, dq2, out);
-        }
-        if (dq1 < 0) {
-            if (dr1 >= 0)
-                return second(q1, r1, p1, p2, r2, q2, dp2, dr2, dq2, out);
-            return second(p1, q1, r1, p2, q2, r2, dp2, dq2, dr2, out);
-        }
-        if (dq1 > 0) {
-            if (dr1 > 0)
-                return second(p1, q1, r1, p2, r2, q2, dp2, dr2, dq2, out);
-            return second(q1, r1, p1, p2, q2, r2, dp2, dq2, dr2, out);
-        }
-        if (dr1 > 0)
-            return second(r1, p1, q1, p2, q2, r2, dp2, dq2, dr2, out);
-        if (dr1 < 0)
-            return second(r1, p1, q1, p2, r2, q2, dp2, dr2, dq2, out);
-        return -1;
+        const int a = rot1 == 0 ? p1 : (rot1 == 1 ? r1 : q1);
+        const int b = rot1 == 0 ? q1 : (rot1 == 1 ? p1 : r1);
+        const int c = rot1 == 0 ? r1 : (rot1 == 1 ? q1 : p1);
+        int v[6];
+        if (!second(a, b, c, p2, sw2 ? r2 : q2, sw2 ? q2 : r2, dp2, sw2 ? dr2 : dq2, sw2 ? dq2 : dr2, v))
+            return -1;
+        return construct(v, out);
     }
 };
 
