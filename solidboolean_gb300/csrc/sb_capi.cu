@@ -595,12 +595,13 @@ sb_status combine_impl(sb_boolean *b)
     int *faceNedges = (int *)(fb + o_fne), *retriRank = (int *)(fb + o_rr);
     SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
     long long totals[4] = {0, 0, 0, 0};
+    int maxNp = 0; // largest pair count of a face
     if (nFaces > 0) {
         SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
         }));
-        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s);
+        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s, d_scalar);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, scratchBytes, scratchOff, nFaces + 1, s);
         }));
@@ -619,6 +620,7 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(cudaMemcpyAsync(&pTot, ptOff + nFaces, sizeof pTot, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaMemcpyAsync(&tTot, triOff + nFaces, sizeof tTot, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaMemcpyAsync(&eTot, edgeOff + nFaces, sizeof eTot, cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaMemcpyAsync(&maxNp, d_scalar, sizeof maxNp, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaStreamSynchronize(s));
         totals[0] = (long long)sTot;
         totals[1] = pTot;
@@ -658,6 +660,8 @@ sb_status combine_impl(sb_boolean *b)
         fa.faceNpts = faceNpts;
         fa.faceNtris = faceNtris;
         fa.faceNedges = faceNedges;
+        static const int smemLimit = face_smem_np_limit();
+        fa.smemNp = std::min(maxNp, smemLimit);
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }
@@ -912,7 +916,6 @@ sb_status combine_impl(sb_boolean *b)
         cudaEventElapsedTime(&ms, b->ev[k], b->ev[k + 1]);
         st.stage_ms[k] = ms;
     }
-    (void)d_scalar;
     b->status = status;
     b->combined = true;
     return status;
