@@ -445,7 +445,6 @@ sb_status combine_impl(sb_boolean *b)
     unsigned int *d_count = reinterpret_cast<unsigned int *>(b->small.as<char>() + 128);
     unsigned int *d_counters = reinterpret_cast<unsigned int *>(b->small.as<char>() + 256);
     int *d_firstFail = reinterpret_cast<int *>(b->small.as<char>() + 512);
-    int *d_scalar = reinterpret_cast<int *>(b->small.as<char>() + 640);
     SB_CUDA_CHECK(cudaMemsetAsync(b->small.ptr, 0, 1024, s));
 
     const int nA = A.nt, nB = B.nt;
@@ -595,13 +594,12 @@ sb_status combine_impl(sb_boolean *b)
     int *faceNedges = (int *)(fb + o_fne), *retriRank = (int *)(fb + o_rr);
     SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
     long long totals[4] = {0, 0, 0, 0};
-    int maxNp = 0; // largest pair count of a face
     if (nFaces > 0) {
         SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
         }));
-        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s, d_scalar);
+        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, scratchBytes, scratchOff, nFaces + 1, s);
         }));
@@ -620,7 +618,6 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(cudaMemcpyAsync(&pTot, ptOff + nFaces, sizeof pTot, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaMemcpyAsync(&tTot, triOff + nFaces, sizeof tTot, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaMemcpyAsync(&eTot, edgeOff + nFaces, sizeof eTot, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaMemcpyAsync(&maxNp, d_scalar, sizeof maxNp, cudaMemcpyDeviceToHost, s));
         SB_CUDA_CHECK(cudaStreamSynchronize(s));
         totals[0] = (long long)sTot;
         totals[1] = pTot;
@@ -660,8 +657,6 @@ sb_status combine_impl(sb_boolean *b)
         fa.faceNpts = faceNpts;
         fa.faceNtris = faceNtris;
         fa.faceNedges = faceNedges;
-        static const int smemLimit = face_smem_np_limit();
-        fa.smemNp = std::min(maxNp, smemLimit);
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }

@@ -602,23 +602,23 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
     return res;
 }
 
-// One face per block of one warp (lane 0 runs it: faces differ in control flow, so packing them into lanes
-// would serialise their paths). The face's scratch lives in the block's shared memory when it fits, so its
-// thousands of dependent accesses do not each go to DRAM; larger faces use their global scratch.
+// Faces per warp. A face is a long serial chain of FP64 operations and FP64 issue is the limit (a warp
+// instruction occupies the FP64 pipe however few of its lanes are active), so lanes should share
+// instructions; but faces differ in control flow, and beyond two per warp their divergent paths cost more
+// than the shared issue saves (measured: 1, 2, 4, 8 faces per warp).
+constexpr int kFacesPerWarp = 2;
+
 __global__ void __launch_bounds__(32) k_faces(FaceArgs a)
 {
-    extern __shared__ __align__(16) char faceSmem[];
-    const int f = blockIdx.x;
-    if (f >= a.nFaces || threadIdx.x != 0)
+    const int f = blockIdx.x * kFacesPerWarp + threadIdx.x;
+    if (threadIdx.x >= kFacesPerWarp || f >= a.nFaces)
         return;
     FaceJob job;
     job.side = a.faceSide[f];
     job.tri = a.faceTri[f];
     job.pairBegin = a.faceBegin[f];
     job.pairEnd = a.faceBegin[f + 1];
-    const int np = job.pairEnd - job.pairBegin;
-    char *base = np <= a.smemNp ? faceSmem : a.scratch + a.scratchOff[f];
-    FaceOut r = process_face(job, a, f, base);
+    FaceOut r = process_face(job, a, f, a.scratch + a.scratchOff[f]);
     a.faceStatus[f] = r.status;
     a.faceNpts[f] = r.npts;
     a.faceNtris[f] = r.status == 0 ? r.ntris : 0;
@@ -627,14 +627,12 @@ __global__ void __launch_bounds__(32) k_faces(FaceArgs a)
 
 // per-face capacities: scratch bytes, points, triangles, edges (written as counts; scanned by the caller)
 __global__ void k_face_sizes(int nFaces, const int *__restrict__ faceBegin, unsigned long long *scratchBytes,
-                             int *ptCap, int *triCap, int *edgeCap, int *maxNp)
+                             int *ptCap, int *triCap, int *edgeCap)
 {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nFaces)
         return;
     int np = faceBegin[f + 1] - faceBegin[f];
-    if (maxNp)
-        atomicMax(maxNp, np);
     scratchBytes[f] = (unsigned long long)face_scratch_bytes_dev(np);
     ptCap[f] = 2 * np;
     triCap[f] = 32 * np + 16;
@@ -642,32 +640,20 @@ __global__ void k_face_sizes(int nFaces, const int *__restrict__ faceBegin, unsi
 }
 
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
-                       int *edgeCap, cudaStream_t s, int *maxNp)
+                       int *edgeCap, cudaStream_t s)
 {
     if (nFaces <= 0)
         return;
-    SB_COUNT(k_face_sizes)<<<(nFaces + 255) / 256, 256, 0, s>>>(nFaces, faceBegin, scratchBytes, ptCap, triCap, edgeCap,
-                                                               maxNp);
+    SB_COUNT(k_face_sizes)<<<(nFaces + 255) / 256, 256, 0, s>>>(nFaces, faceBegin, scratchBytes, ptCap, triCap, edgeCap);
 }
 
-// shared memory a face block may take: several such blocks stay resident per SM
-constexpr size_t kFaceSmemMax = 48 * 1024;
-
-int face_smem_np_limit()
-{
-    int np = 0;
-    while (np < 4096 && face_scratch_bytes_host(np + 1) <= kFaceSmemMax)
-        ++np;
-    return np;
-}
 
 void launch_faces(const FaceArgs &a, cudaStream_t s)
 {
     if (a.nFaces <= 0)
         return;
     KTime kt("k_faces", s);
-    const size_t smem = a.smemNp > 0 ? face_scratch_bytes_host(a.smemNp) : 0;
-    SB_COUNT(k_faces)<<<a.nFaces, 32, smem, s>>>(a);
+    SB_COUNT(k_faces)<<<(a.nFaces + kFacesPerWarp - 1) / kFacesPerWarp, 32, 0, s>>>(a);
 }
 
 } // namespace sbg

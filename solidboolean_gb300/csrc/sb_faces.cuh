@@ -24,15 +24,11 @@ struct FaceArgs {
     int *faceTris;                             // local ids, 3 per triangle
     int *faceEdges;                            // local ids, 2 per edge
     int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
-    int smemNp = 0; // faces with at most this many pairs keep their scratch in shared memory (0: none)
 };
 
 size_t face_scratch_bytes_host(int np);
-// maxNp (optional, device int set to 0 beforehand) receives the largest pair count of any face
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
-                       int *edgeCap, cudaStream_t s, int *maxNp = nullptr);
-// largest pair count whose face scratch fits the shared memory one face block may use
-int face_smem_np_limit();
+                       int *edgeCap, cudaStream_t s);
 void launch_faces(const FaceArgs &a, cudaStream_t s);
 
 } // namespace sbg

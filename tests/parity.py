@@ -108,12 +108,18 @@ def compare(oracle: dict, gpu: dict, n_orig: int, factor: int, coord_rtol: float
     err = np.where(vo == vg, 0.0, err)
     if err.size and float(err.max()) > coord_rtol:
         bad["coordinates"] = float(err.max())
-    for op_name in ("union", "diff", "intersect"):
-        a = canonical_tris(oracle[op_name], ro)
-        b = canonical_tris(gpu[op_name], rg)
-        if a.shape != b.shape or not np.array_equal(a, b):
-            bad[op_name] = (len(a), len(b))
+    # the arrangement's triangles as a set; what is inside or outside (labels, and the fetched
+    # operations built from them) only when asked
+    at = canonical_tris(oracle["newt"], ro)
+    bt = canonical_tris(gpu["newt"], rg)
+    if at.shape != bt.shape or not np.array_equal(at, bt):
+        bad["arrangement"] = (len(at), len(bt))
     if check_labels:
+        for op_name in ("union", "diff", "intersect"):
+            a = canonical_tris(oracle[op_name], ro)
+            b = canonical_tris(gpu[op_name], rg)
+            if a.shape != b.shape or not np.array_equal(a, b):
+                bad[op_name] = (len(a), len(b))
         lo = labelled_tris(oracle["newt"], oracle_labels(oracle), ro)
         lg = labelled_tris(gpu["newt"], gpu["labels"], rg)
         if lo.shape != lg.shape or not np.array_equal(lo, lg):
