@@ -152,7 +152,8 @@ def workload():
     return mg.pair_large(SEED, LEVEL)
 
 
-# algorithmic bytes per launch of the instrumented kernels (per unit x units)
+# algorithmic bytes per launch of the instrumented kernels (per unit x units; the leaf-order kernels run
+# once per mesh, so their figure is the mean over the two meshes)
 def kernel_bytes(name: str, st: dict, na: int, nb: int, nva: int, nvb: int) -> float:
     C, K = st["candidate_pairs"], st["intersecting_pairs"]
     F = st["cut_faces_first"] + st["cut_faces_second"]
@@ -171,7 +172,26 @@ def kernel_bytes(name: str, st: dict, na: int, nb: int, nva: int, nvb: int) -> f
         # union-find: read the triangle, three key lookups (12 B) and twin lookups (12 B), parent writes
         "k_union": (12 + 3 * 12 + 3 * 12 + 8) * float(T),
         "k_uf_flatten": 8.0 * T,
+        # reference leaf order, large-node phase: every level reads each triangle's state word and the
+        # integer record fields it classifies and reduces (centre key on the split axis, box keys and
+        # fixed-point centre: 80 B) and writes the state back (8 B); levels = ceil(log2(n / 1024)) + 1
+        "k_rr_top": 0.5 * 88.0 * (na * rr_levels(na) + nb * rr_levels(nb)),
+        # subtree phase: sorted member index and Morton position (8 B), the record fields per level (80 B,
+        # about log2(1024 / 20) + 1 levels) and the final position (4 B)
+        "k_rr_subtree": 0.5 * (na + nb) * (8.0 + 80.0 * 7 + 4.0),
+        # records: three vertex indices (12 B), nine coordinates (72 B), the FP64 box (48 B); writes the
+        # 96 B record, its structure-of-arrays copy (96 B) and the position and state words (8 B)
+        "k_rr_elems": 0.5 * (na + nb) * (12.0 + 72.0 + 48.0 + 96.0 + 96.0 + 8.0),
     }.get(name, 0.0)
+
+
+def rr_levels(n: int) -> int:
+    """levels of the reference tree's large-node phase for n triangles (nodes above 1024 members split)"""
+    levels = 1
+    while n > 1024:
+        n = (n + 1) // 2
+        levels += 1
+    return levels
 
 
 def gpu_arm(args, rank, world, local, dist):

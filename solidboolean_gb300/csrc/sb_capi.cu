@@ -1117,6 +1117,13 @@ void sb_mesh_destroy(sb_mesh *m)
         return;
     m->buf.release();
     m->tmp.release();
+    m->rankTmp.release();
+    if (m->aux)
+        cudaStreamDestroy(m->aux);
+    if (m->auxFork)
+        cudaEventDestroy(m->auxFork);
+    if (m->auxJoin)
+        cudaEventDestroy(m->auxJoin);
     delete m;
 }
 

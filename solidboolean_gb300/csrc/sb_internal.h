@@ -61,7 +61,10 @@ struct sb_mesh_impl;
 struct sb_mesh {
     sbg::MeshDev d;
     sbg::DevBuf buf;
-    sbg::DevBuf tmp;
+    sbg::DevBuf tmp;               // LBVH build temporaries
+    sbg::DevBuf rankTmp;           // reference leaf-order temporaries (built concurrently with the LBVH)
+    cudaStream_t aux = nullptr;    // second stream of the preparation, created on first use
+    cudaEvent_t auxFork = nullptr, auxJoin = nullptr;
     bool prepared = false;
     bool ownsInput = true;
     cudaStream_t stream = nullptr;

@@ -291,6 +291,18 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     SB_COUNT(k_morton)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tb + t_cub, sortBytes, keyIn, d.morton, idxIn, d.leafTri, nt, 0,
                                                   30, s));
+    // The reference leaf order needs only the boxes and the Morton order: it runs on a second stream while
+    // this one builds and refits the LBVH.
+    const bool fork = order_mode == SB_ORDER_REFERENCE;
+    if (fork) {
+        if (!m->aux) {
+            SB_CUDA_CHECK(cudaStreamCreateWithFlags(&m->aux, cudaStreamNonBlocking));
+            SB_CUDA_CHECK(cudaEventCreateWithFlags(&m->auxFork, cudaEventDisableTiming));
+            SB_CUDA_CHECK(cudaEventCreateWithFlags(&m->auxJoin, cudaEventDisableTiming));
+        }
+        SB_CUDA_CHECK(cudaEventRecord(m->auxFork, s));
+        SB_CUDA_CHECK(cudaStreamWaitEvent(m->aux, m->auxFork, 0));
+    }
     if (nt > 1) {
         SB_CUDA_CHECK(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * 2 * (size_t)nt, s));
         SB_CUDA_CHECK(cudaMemsetAsync(d.flags, 0, sizeof(int) * (size_t)(nt - 1), s));
@@ -303,8 +315,10 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     }
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = false;
-    if (order_mode == SB_ORDER_REFERENCE) {
-        sb_status st = build_reference_rank(m, s);
+    if (fork) {
+        sb_status st = build_reference_rank(m, m->aux); // returns once its own stream has finished
+        SB_CUDA_CHECK(cudaEventRecord(m->auxJoin, m->aux));
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
         if (st != SB_OK)
             return st;
     }

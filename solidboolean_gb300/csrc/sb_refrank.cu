@@ -1282,7 +1282,6 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     d.rankValid = false;
     if (nt <= 0)
         return SB_OK;
-    KTime kt("reference_leaf_order", s);
     // large nodes have more than kSub members and are disjoint within a level
     const int maxNodes = 16 * (nt / kSub) + 256;
     const int keyBits = bit_length(nt);
@@ -1297,8 +1296,8 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     const size_t o_np = c.take<NParam>(maxNodes);
     const size_t o_nodes = c.take<RNode>(maxNodes), o_terms = c.take<int>(maxNodes), o_ct = c.take<int>(kCtCount),
                  o_sc = c.take<int>(4), o_bar = c.take<GridBar>(1), o_cub = c.take<char>(sortBytes);
-    SB_CUDA_CHECK(m->tmp.ensure(c.off));
-    char *b = m->tmp.as<char>();
+    SB_CUDA_CHECK(m->rankTmp.ensure(c.off));
+    char *b = m->rankTmp.as<char>();
     RRec *rec = (RRec *)(b + o_rec);
     unsigned long long *soa = (unsigned long long *)(b + o_soa);
     int *state = (int *)(b + o_state);
@@ -1311,8 +1310,11 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
 
     const int GE = (nt + kElemThreads - 1) / kElemThreads;
     SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters, reinterpret_cast<unsigned *>(bar));
-    SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, soa, posOf, state,
-                                                      nodes);
+    {
+        KTime kt("k_rr_elems", s);
+        SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, soa, posOf, state,
+                                                          nodes);
+    }
     SB_COUNT(k_rr_root_sum)<<<GE, kElemThreads, 0, s>>>(nt, rec, soa, nodes, scg);
     SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, np, nt, scg, counters, terms);
     // the large-node phase: one cooperative launch, every block resident
@@ -1323,6 +1325,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
         void *args[] = {(void *)&nt, (void *)&rec, (void *)&soa, (void *)&state, (void *)&np, (void *)&nodes, (void *)&counters,
                         (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar};
         count_launch();
+        KTime kt("k_rr_top", s);
         SB_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)k_rr_top, dim3(topBlocks), dim3(kElemThreads), args, 0, s));
     }
     SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
@@ -1330,8 +1333,11 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
     SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem));
     // one block per terminal node; the count is known only on the device, so the grid covers every node record
     // that could be terminal and the surplus blocks return at once
-    SB_COUNT(k_rr_subtree)<<<maxNodes, kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri, scg,
-                                                                    d.rank, counters);
+    {
+        KTime kt("k_rr_subtree", s);
+        SB_COUNT(k_rr_subtree)<<<maxNodes, kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri,
+                                                                        scg, d.rank, counters);
+    }
     int cnt[kCtCount];
     GridBar hb;
     SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
