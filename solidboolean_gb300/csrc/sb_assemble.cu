@@ -20,39 +20,6 @@
 
 namespace sbg {
 
-// ---------------------------------------------------------------------------------------------------
-// hash tables (open addressing, linear probing, power-of-two capacity)
-// ---------------------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t slot_of(uint64_t h, uint32_t mask) { return (uint32_t)(mix64(h) & mask); }
-
-// map uint64 key -> min(int value)
-__device__ void u64map_insert_min(uint64_t *keys, int *vals, uint32_t mask, uint64_t key, int val)
-{
-    uint32_t s = slot_of(key, mask);
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        uint64_t prev = atomicCAS((unsigned long long *)(keys + s), (unsigned long long)kEmpty64,
-                                  (unsigned long long)key);
-        if (prev == kEmpty64 || prev == key) {
-            atomicMin(vals + s, val);
-            return;
-        }
-        s = (s + 1) & mask;
-    }
-}
-__device__ int u64map_find(const uint64_t *keys, const int *vals, uint32_t mask, uint64_t key)
-{
-    uint32_t s = slot_of(key, mask);
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        uint64_t k = keys[s];
-        if (k == key)
-            return vals[s];
-        if (k == kEmpty64)
-            return -1;
-        s = (s + 1) & mask;
-    }
-    return -1;
-}
-
 // ---- global weld ------------------------------------------------------------------------------------
 // seq = position of a cut point in (face order, local order); slots claim by the first seq to arrive and
 // keep the minimum seq of the key
@@ -125,12 +92,14 @@ __global__ void k_mark_cut(int nFaces, const int *__restrict__ faceSide, const i
 
 // uncut triangles of one mesh, in index order, offset into the arrangement
 __global__ void k_uncut(int nt, const uint32_t *__restrict__ t, const int *__restrict__ cut,
-                        const int *__restrict__ uncutRank, uint32_t vbase, uint32_t outBase, uint32_t *newT)
+                        const int *__restrict__ uncutRank, uint32_t vbase, uint32_t outBase, uint32_t *newT,
+                        int *origUncut)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nt || cut[i])
         return;
     uint32_t o = outBase + (uint32_t)uncutRank[i];
+    origUncut[o] = i;
     newT[3 * (size_t)o] = t[3 * (size_t)i] + vbase;
     newT[3 * (size_t)o + 1] = t[3 * (size_t)i + 1] + vbase;
     newT[3 * (size_t)o + 2] = t[3 * (size_t)i + 2] + vbase;
@@ -149,7 +118,7 @@ __global__ void k_retri(int nFaces, const int *__restrict__ faceSide, const int 
                         const int *__restrict__ retriRank, const int *__restrict__ faceTris,
                         const int *__restrict__ ptOff, const int *__restrict__ pointSlot,
                         const int *__restrict__ slotRank, MeshDev A, MeshDev B, uint32_t newBase, uint32_t outBase,
-                        uint32_t *newT)
+                        uint32_t *newT, int *retriFace)
 {
     int f = blockIdx.x;
     if (f >= nFaces)
@@ -161,6 +130,7 @@ __global__ void k_retri(int nFaces, const int *__restrict__ faceSide, const int 
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const int *lt = faceTris + 3 * (size_t)(triOff[f] + k);
         uint32_t o = outBase + (uint32_t)(retriRank[f] + k);
+        retriFace[retriRank[f] + k] = f;
         for (int c = 0; c < 3; ++c)
             newT[3 * (size_t)o + c] = local_to_global(lt[c], tri, vbase, ptOff[f], pointSlot, slotRank, newBase);
     }
@@ -212,7 +182,6 @@ __global__ void k_loop_check(int n, const int *__restrict__ degree, unsigned int
 }
 
 // ---- half-edge tables, union-find ---------------------------------------------------------------------
-__device__ __forceinline__ uint64_t he_key(uint32_t a, uint32_t b) { return ((uint64_t)a << 32) | b; }
 
 __global__ void k_halfedges(int nTri, const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh,
                             uint64_t *keysA, int *valsA, uint64_t *keysB, int *valsB, uint32_t mask)
@@ -294,6 +263,94 @@ __global__ void k_union(int nTri, const uint32_t *__restrict__ newT, const int8_
         int tw = u64map_find(keys, vals, mask, he_key(b, a));
         if (tw >= 0)
             uf_union(parent, t, tw);
+    }
+    seedFlag[t] = seed;
+}
+
+// Grouping through the input adjacency (both input meshes hold every directed edge once). The per-mesh
+// half-edge tables hold only the re-triangulated triangles (first owner wins; the meshes need separate tables
+// because the cut points are shared vertices of both). The twin of an uncut triangle's edge is its input neighbour when that one is
+// uncut, else a re-triangulated triangle of the neighbour found in the table; the twin of a re-triangulated
+// triangle's edge is found in the table, or, on an original edge of its face, is the uncut neighbour across
+// it. With every directed edge held once per mesh this crosses exactly the half-edges k_union crosses.
+__global__ void k_halfedges_retri(int nRetri, int retriBase, const uint32_t *__restrict__ newT,
+                                  const int8_t *__restrict__ triMesh, uint64_t *keysA, int *valsA, uint64_t *keysB,
+                                  int *valsB, uint32_t mask)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nRetri)
+        return;
+    const int t = retriBase + r;
+    const uint32_t *v = newT + 3 * (size_t)t;
+    uint64_t *keys = triMesh[t] == 0 ? keysA : keysB;
+    int *vals = triMesh[t] == 0 ? valsA : valsB;
+    for (int i = 0; i < 3; ++i)
+        u64map_insert_min(keys, vals, mask, he_key(v[i], v[(i + 1) % 3]), t);
+}
+
+__global__ void k_union_adj(int nTri, int uncutA, int uncutB, const uint32_t *__restrict__ newT,
+                            const int8_t *__restrict__ triMesh, const int *__restrict__ origUncut,
+                            const int *__restrict__ retriFace, const int *__restrict__ faceTri, MeshDev A, MeshDev B,
+                            const int *__restrict__ cutA, const int *__restrict__ cutB,
+                            const int *__restrict__ uncutRankA, const int *__restrict__ uncutRankB,
+                            const uint64_t *keysA, const int *valsA, const uint64_t *keysB, const int *valsB,
+                            uint32_t mask, const uint64_t *edgeKeys,
+                            const int *edgeVals, uint32_t emask, uint32_t newBase, int *parent, int *seedFlag,
+                            unsigned int *dupCount)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nTri)
+        return;
+    const int retriBase = uncutA + uncutB;
+    const uint32_t *v = newT + 3 * (size_t)t;
+    const int side = triMesh[t];
+    const MeshDev &M = side == 0 ? A : B;
+    const int *cut = side == 0 ? cutA : cutB;
+    const int *urank = side == 0 ? uncutRankA : uncutRankB;
+    const int outBase = side == 0 ? 0 : uncutA;
+    const uint32_t vbase = side == 0 ? 0u : (uint32_t)A.nv;
+    const uint64_t *keys = side == 0 ? keysA : keysB;
+    const int *vals = side == 0 ? valsA : valsB;
+    int seed = 0;
+    if (t < retriBase) {
+        const int i = origUncut[t];
+        for (int k = 0; k < 3; ++k) {
+            const int j = M.adj[3 * (size_t)i + k];
+            if (j < 0)
+                continue;
+            const int tw = !cut[j] ? outBase + urank[j]
+                                   : u64map_find(keys, vals, mask, he_key(v[(k + 1) % 3], v[k]));
+            if (tw >= 0)
+                uf_union(parent, t, tw);
+        }
+    } else {
+        const int face = faceTri[retriFace[t - retriBase]];
+        const uint32_t *c = M.t + 3 * (size_t)face;
+        for (int i = 0; i < 3; ++i) {
+            const uint32_t a = v[i], b = v[(i + 1) % 3];
+            const int owner = u64map_find(keys, vals, mask, he_key(a, b));
+            if (owner != t)
+                atomicAdd(dupCount, 1u);
+            if (is_cut_edge(edgeKeys, edgeVals, emask, a, b, newBase)) {
+                if (owner == t)
+                    seed = 1;
+                continue;
+            }
+            if (owner != t)
+                continue; // a repeated half-edge was already crossed by its first owner
+            int tw = u64map_find(keys, vals, mask, he_key(b, a));
+            if (tw < 0 && a < newBase && b < newBase) {
+                for (int kk = 0; kk < 3; ++kk)
+                    if (c[kk] + vbase == a && c[(kk + 1) % 3] + vbase == b) {
+                        const int j = M.adj[3 * (size_t)face + kk];
+                        if (j >= 0 && !cut[j])
+                            tw = outBase + urank[j];
+                        break;
+                    }
+            }
+            if (tw >= 0)
+                uf_union(parent, t, tw);
+        }
     }
     seedFlag[t] = seed;
 }
@@ -616,20 +673,21 @@ void launch_arrangement(const AsmArgs &g, cudaStream_t s)
     if (g.A.nt > 0)
         {
             KTime kt("k_uncut", s);
-            SB_COUNT(k_uncut)<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT);
+            SB_COUNT(k_uncut)<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT,
+                                                              g.origUncut);
         }
     if (g.B.nt > 0)
         {
             KTime kt("k_uncut", s);
             SB_COUNT(k_uncut)<<<nb(g.B.nt, 256), 256, 0, s>>>(g.B.nt, g.B.t, g.cutB, g.uncutRankB, (uint32_t)g.A.nv,
-                                                (uint32_t)g.uncutA, g.newT);
+                                                (uint32_t)g.uncutA, g.newT, g.origUncut);
         }
     if (g.nFaces > 0)
         {
             KTime kt("k_retri", s);
             SB_COUNT(k_retri)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceTri, g.faceNtris, g.triOff, g.retriRank,
                                         g.faceTris, g.ptOff, g.pointSlot, g.slotRank, g.A, g.B,
-                                        (uint32_t)g.newBase, (uint32_t)(g.uncutA + g.uncutB), g.newT);
+                                        (uint32_t)g.newBase, (uint32_t)(g.uncutA + g.uncutB), g.newT, g.retriFace);
         }
 }
 
@@ -656,16 +714,31 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nTri <= 0)
         return;
-    {
-        KTime kt("k_halfedges", s);
-        SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
-                                                g.heValsB, g.heMask);
-    }
-    {
+    if (g.useAdj) {
+        const int retriBase = g.uncutA + g.uncutB, nRetri = g.nTri - retriBase;
+        if (nRetri > 0) {
+            KTime kt("k_halfedges", s);
+            SB_COUNT(k_halfedges_retri)<<<nb(nRetri, 256), 256, 0, s>>>(nRetri, retriBase, g.newT, g.triMesh,
+                                                                       g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
+                                                                       g.heMask);
+        }
         KTime kt("k_union", s);
-        SB_COUNT(k_union)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
-                                            g.heMask, g.edgeKeys, g.edgeVals, g.edgeMask, (uint32_t)g.newBase,
-                                            g.parent, g.seedFlag, g.counters + kCntDupHalfedge);
+        SB_COUNT(k_union_adj)<<<nb(g.nTri, 256), 256, 0, s>>>(
+            g.nTri, g.uncutA, g.uncutB, g.newT, g.triMesh, g.origUncut, g.retriFace, g.faceTri, g.A, g.B, g.cutA,
+            g.cutB, g.uncutRankA, g.uncutRankB, g.heKeysA, g.heValsA, g.heKeysB, g.heValsB, g.heMask, g.edgeKeys,
+            g.edgeVals, g.edgeMask,
+            (uint32_t)g.newBase, g.parent, g.seedFlag, g.counters + kCntDupHalfedge);
+    } else {
+        {
+            KTime kt("k_halfedges", s);
+            SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA,
+                                                                 g.heKeysB, g.heValsB, g.heMask);
+        }
+        KTime kt("k_union", s);
+        SB_COUNT(k_union)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
+                                                         g.heValsB, g.heMask, g.edgeKeys, g.edgeVals, g.edgeMask,
+                                                         (uint32_t)g.newBase, g.parent, g.seedFlag,
+                                                         g.counters + kCntDupHalfedge);
     }
     {
         KTime kt("k_uf_flatten", s);

@@ -1,11 +1,10 @@
 // Assembly / labelling launch interface.
 #pragma once
 #include "sb_common.cuh"
+#include "sb_hash.cuh"
 #include "sb_internal.h"
 
 namespace sbg {
-
-constexpr uint64_t kEmpty64 = ~0ull;
 
 // device counters (unsigned int) used by the assembly kernels
 enum {
@@ -50,6 +49,11 @@ struct AsmArgs {
     int *heValsA, *heValsB;
     uint32_t heMask;
     int *parent, *seedFlag, *seedMin, *remMin, *repOfRoot, *reps, *insideCount;
+    // grouping through the input meshes' edge adjacency (both meshes hold every directed edge once): the
+    // per-mesh half-edge tables then hold the re-triangulated triangles only
+    int useAdj;
+    int *origUncut;  // [uncutA + uncutB] input triangle of each uncut arrangement triangle
+    int *retriFace;  // [nTri - uncutA - uncutB] face of each re-triangulated triangle
     int8_t *label;
     unsigned int *counters;
 };

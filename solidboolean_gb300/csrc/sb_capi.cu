@@ -111,6 +111,8 @@ static size_t mesh_bytes(int nv, int nt)
     c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
     c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
     c.take<int>((size_t)nt);
+    c.take<int>((size_t)nt * 3);
+    c.take<int>(1);
     return c.off;
 }
 
@@ -756,7 +758,13 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 2, retriRank + FA, sizeof(int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 3, retriRank + nFaces, sizeof(int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaMemcpyAsync(firstFail, d_firstFail, sizeof firstFail, cudaMemcpyDeviceToHost, s));
+    int adjDup[2] = {1, 1}; // directed edges held twice in an input mesh (grouping then hashes every half-edge)
+    if (A.adj && B.adj) {
+        SB_CUDA_CHECK(cudaMemcpyAsync(adjDup, A.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SB_CUDA_CHECK(cudaMemcpyAsync(adjDup + 1, B.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    g.useAdj = adjDup[0] == 0 && adjDup[1] == 0;
     g.uncutA = cnts[0];
     g.uncutB = cnts[1];
     g.retriRank = retriRank;
@@ -771,6 +779,7 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_F0 = cr.take<uint32_t>(3 * (size_t)nTri + 3), o_F1 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
     size_t o_F2 = cr.take<uint32_t>(3 * (size_t)nTri + 3);
     size_t o_fl = cr.take<int>(3 * ((size_t)nTri + 1)), o_fr2 = cr.take<int>(3 * ((size_t)nTri + 1));
+    size_t o_ou = cr.take<int>((size_t)cnts[0] + cnts[1] + 1), o_rf = cr.take<int>((size_t)cnts[3] + 1);
     SB_CUDA_CHECK(b->res.ensure(cr.off));
     char *rb = b->res.as<char>();
     g.newV = (double *)(rb + o_V);
@@ -778,6 +787,8 @@ sb_status combine_impl(sb_boolean *b)
     g.label = (int8_t *)(rb + o_L);
     g.triMesh = (int8_t *)(rb + o_M);
     g.isUncut = (int8_t *)(rb + o_U);
+    g.origUncut = (int *)(rb + o_ou);
+    g.retriFace = (int *)(rb + o_rf);
     b->d_newV = g.newV;
     b->nNewV = nV;
     b->d_newT = g.newT;
@@ -799,7 +810,9 @@ sb_status combine_impl(sb_boolean *b)
 
     // ---------------- cut loops, groups, sides ----------------
     const uint32_t edgeCapH = pow2_at_least(2 * (size_t)totals[3] + 2);
-    const uint32_t heCap = pow2_at_least(2 * 3 * (size_t)nTri + 2);
+    // per-mesh half-edge tables: every arrangement triangle's, or through the input adjacency only the
+    // re-triangulated triangles'
+    const uint32_t heCap = pow2_at_least(2 * 3 * (size_t)(g.useAdj ? cnts[3] : nTri) + 2);
     Carve cg2;
     size_t o_ek = cg2.take<uint64_t>(edgeCapH), o_ev = cg2.take<int>(edgeCapH), o_dg = cg2.take<int>(nNew + 1);
     size_t o_hkA = cg2.take<uint64_t>(heCap), o_hvA = cg2.take<int>(heCap);

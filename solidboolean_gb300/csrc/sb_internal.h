@@ -52,6 +52,10 @@ struct MeshDev {
     int *flags = nullptr;     // [nt-1] refit arrival counters
     int *rank = nullptr;      // [nt] position of each triangle in the reference tree's leaf order
     bool rankValid = false;
+    // [nt*3] for edge k of triangle i (t[k] -> t[k+1]): the first triangle in index order holding the reverse
+    // edge, -1 for none. Depends on the triangles only, so a vertex update keeps it.
+    int *adj = nullptr;
+    int *adjDup = nullptr;    // [1] directed edges held by more than one triangle (0: every edge once)
     int root = 0;             // 0, or ~0 when nt == 1
 };
 
@@ -66,6 +70,7 @@ struct sb_mesh {
     cudaStream_t aux = nullptr;    // second stream of the preparation, created on first use
     cudaEvent_t auxFork = nullptr, auxJoin = nullptr;
     bool prepared = false;
+    bool adjValid = false;         // adj / adjDup computed for the current triangles
     bool ownsInput = true;
     cudaStream_t stream = nullptr;
     std::vector<double> hostV;    // only for host-created meshes (kept for re-preparation)

@@ -11,6 +11,7 @@
 #include <cub/cub.cuh>
 
 #include "sb_common.cuh"
+#include "sb_hash.cuh"
 #include "sb_internal.h"
 
 namespace sbg {
@@ -217,6 +218,43 @@ __global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__
 
 static inline int blocks_for(size_t n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// Edge adjacency of the input triangles: every directed edge (a -> b) into a table that keeps its first
+// triangle in index order; then each edge's reverse (b -> a) looked up. This is the half-edge map the
+// reference builds over the arrangement (src/solidboolean.cpp:167-239) restricted to one input mesh, so the
+// grouping can read the twins of uncut triangles directly instead of hashing all of their half-edges.
+static uint32_t adj_capacity(int nt)
+{
+    uint32_t p = 1024;
+    while (p < 2ull * 3ull * (uint64_t)nt)
+        p <<= 1;
+    return p;
+}
+
+__global__ void k_adj_insert(int nt, const uint32_t *__restrict__ t, uint64_t *keys, int *vals, uint32_t mask)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt)
+        return;
+    const uint32_t v[3] = {t[3 * (size_t)i], t[3 * (size_t)i + 1], t[3 * (size_t)i + 2]};
+    for (int k = 0; k < 3; ++k)
+        u64map_insert_min(keys, vals, mask, he_key(v[k], v[(k + 1) % 3]), i);
+}
+
+__global__ void k_adj_find(int nt, const uint32_t *__restrict__ t, const uint64_t *__restrict__ keys,
+                           const int *__restrict__ vals, uint32_t mask, int *adj, int *adjDup)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt)
+        return;
+    const uint32_t v[3] = {t[3 * (size_t)i], t[3 * (size_t)i + 1], t[3 * (size_t)i + 2]};
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t a = v[k], b = v[(k + 1) % 3];
+        if (u64map_find(keys, vals, mask, he_key(a, b)) != i)
+            atomicAdd(adjDup, 1);
+        adj[3 * (size_t)i + k] = u64map_find(keys, vals, mask, he_key(b, a));
+    }
+}
+
 sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
 {
     MeshDev &d = m->d;
@@ -240,6 +278,8 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     size_t o_n64 = c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
     size_t o_fl = c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
     size_t o_rk = c.take<int>((size_t)nt);
+    size_t o_adj = c.take<int>((size_t)nt * 3);
+    size_t o_ad = c.take<int>(1);
     (void)o_v;
     (void)o_t;
     if (m->buf.bytes < c.off) {
@@ -250,6 +290,7 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
         SB_CUDA_CHECK(cudaStreamSynchronize(s));
         m->buf.release();
         m->buf = nb;
+        m->adjValid = false;
         d.v = m->buf.as<double>();
         d.t = reinterpret_cast<uint32_t *>(m->buf.as<char>() + o_t);
     }
@@ -265,6 +306,8 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     d.nbox64 = reinterpret_cast<double *>(base + o_n64);
     d.flags = reinterpret_cast<int *>(base + o_fl);
     d.rank = reinterpret_cast<int *>(base + o_rk);
+    d.adj = reinterpret_cast<int *>(base + o_adj);
+    d.adjDup = reinterpret_cast<int *>(base + o_ad);
 
     // temporaries: centres, bounds, unsorted keys/indices, CUB scratch
     size_t sortBytes = 0;
@@ -276,6 +319,9 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     size_t t_key = tc.take<uint32_t>((size_t)nt);
     size_t t_idx = tc.take<int>((size_t)nt);
     size_t t_cub = tc.take<char>(sortBytes);
+    const uint32_t adjCap = adj_capacity(nt);
+    size_t t_ak = m->adjValid ? 0 : tc.take<uint64_t>(adjCap);
+    size_t t_av = m->adjValid ? 0 : tc.take<int>(adjCap);
     SB_CUDA_CHECK(m->tmp.ensure(tc.off));
     char *tb = m->tmp.as<char>();
     float *cen = reinterpret_cast<float *>(tb + t_cen);
@@ -312,6 +358,16 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
         d.root = 0;
     } else {
         d.root = ~0;
+    }
+    if (!m->adjValid) {
+        uint64_t *ak = reinterpret_cast<uint64_t *>(tb + t_ak);
+        int *av = reinterpret_cast<int *>(tb + t_av);
+        SB_CUDA_CHECK(cudaMemsetAsync(ak, 0xFF, sizeof(uint64_t) * adjCap, s));
+        SB_CUDA_CHECK(cudaMemsetAsync(av, 0x7F, sizeof(int) * adjCap, s)); // above any triangle index
+        SB_CUDA_CHECK(cudaMemsetAsync(d.adjDup, 0, sizeof(int), s));
+        SB_COUNT(k_adj_insert)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.t, ak, av, adjCap - 1);
+        SB_COUNT(k_adj_find)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.t, ak, av, adjCap - 1, d.adj, d.adjDup);
+        m->adjValid = true;
     }
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = false;

@@ -14,7 +14,23 @@ CASES = {
     "near_tangent_L4": lambda: mg.near_tangent(1234, level=4),
     "pair_large_L4": lambda: mg.pair_large(1234, level=4),
     "diff_volume_L3": lambda: mg.diff_volume(1234, level=3)[:4],
+    # meshes that hold a directed edge twice: the grouping cannot use the input adjacency and hashes every
+    # half-edge of the arrangement, as the reference does
+    "pair_small_flipped_triangle": lambda: _flipped(mg.pair_small(1234), 5),
+    "pair_small_repeated_triangle": lambda: _repeated(mg.pair_small(1234), 7),
 }
+
+
+def _flipped(pair, i):
+    va, fa, vb, fb = pair
+    fa = fa.copy()
+    fa[i] = fa[i][::-1]
+    return va, fa, vb, fb
+
+
+def _repeated(pair, i):
+    va, fa, vb, fb = pair
+    return va, np.vstack([fa, fa[i:i + 1]]), vb, fb
 
 
 @pytest.mark.parametrize("precision", ["filtered", "fp64"])
