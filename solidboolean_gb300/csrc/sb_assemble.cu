@@ -93,10 +93,10 @@ __global__ void k_mark_cut(int nFaces, const int *__restrict__ faceSide, const i
 // uncut triangles of one mesh, in index order, offset into the arrangement
 __global__ void k_uncut(int nt, const uint32_t *__restrict__ t, const int *__restrict__ cut,
                         const int *__restrict__ uncutRank, uint32_t vbase, uint32_t outBase, uint32_t *newT,
-                        int *origUncut)
+                        int *origUncut, const int *__restrict__ truncOcc)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nt || cut[i])
+    if (i >= nt || cut[i] || i > *truncOcc / 3)
         return;
     uint32_t o = outBase + (uint32_t)uncutRank[i];
     origUncut[o] = i;
@@ -184,15 +184,19 @@ __global__ void k_loop_check(int n, const int *__restrict__ degree, unsigned int
 // ---- half-edge tables, union-find ---------------------------------------------------------------------
 
 __global__ void k_halfedges(int nTri, const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh,
-                            uint64_t *keysA, int *valsA, uint64_t *keysB, int *valsB, uint32_t mask)
+                            uint64_t *keysA, int *valsA, uint64_t *keysB, int *valsB, uint32_t mask, int uncutAll,
+                            const int *__restrict__ origUncut, const int *__restrict__ truncOcc)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nTri)
         return;
     const uint32_t *v = newT + 3 * (size_t)t;
-    uint64_t *keys = triMesh[t] == 0 ? keysA : keysB;
-    int *vals = triMesh[t] == 0 ? valsA : valsB;
-    for (int i = 0; i < 3; ++i)
+    const int m = triMesh[t];
+    uint64_t *keys = m == 0 ? keysA : keysB;
+    int *vals = m == 0 ? valsA : valsB;
+    // the last uncut triangle of a truncated mesh inserted its half-edges only up to the repeated one
+    const int lastEdge = t < uncutAll ? truncOcc[m] - 3 * origUncut[t] : 2;
+    for (int i = 0; i < 3 && i <= lastEdge; ++i)
         u64map_insert_min(keys, vals, mask, he_key(v[i], v[(i + 1) % 3]), t);
 }
 
@@ -674,13 +678,13 @@ void launch_arrangement(const AsmArgs &g, cudaStream_t s)
         {
             KTime kt("k_uncut", s);
             SB_COUNT(k_uncut)<<<nb(g.A.nt, 256), 256, 0, s>>>(g.A.nt, g.A.t, g.cutA, g.uncutRankA, 0u, 0u, g.newT,
-                                                              g.origUncut);
+                                                              g.origUncut, g.truncOcc);
         }
     if (g.B.nt > 0)
         {
             KTime kt("k_uncut", s);
             SB_COUNT(k_uncut)<<<nb(g.B.nt, 256), 256, 0, s>>>(g.B.nt, g.B.t, g.cutB, g.uncutRankB, (uint32_t)g.A.nv,
-                                                (uint32_t)g.uncutA, g.newT, g.origUncut);
+                                                (uint32_t)g.uncutA, g.newT, g.origUncut, g.truncOcc + 1);
         }
     if (g.nFaces > 0)
         {
@@ -732,7 +736,8 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
         {
             KTime kt("k_halfedges", s);
             SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA,
-                                                                 g.heKeysB, g.heValsB, g.heMask);
+                                                                 g.heKeysB, g.heValsB, g.heMask,
+                                                                 g.uncutA + g.uncutB, g.origUncut, g.truncOcc);
         }
         KTime kt("k_union", s);
         SB_COUNT(k_union)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,

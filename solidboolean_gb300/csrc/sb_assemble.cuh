@@ -53,6 +53,10 @@ struct AsmArgs {
     // per-mesh half-edge tables then hold the re-triangulated triangles only
     int useAdj;
     int *origUncut;  // [uncutA + uncutB] input triangle of each uncut arrangement triangle
+    // [2] per mesh, 3 i + k of the first uncut triangle edge whose half-edge repeats an earlier one (INT_MAX:
+    // none): the reference stops adding that mesh's uncut triangles there, keeping triangle i and the
+    // half-edges inserted before the repeat (src/solidboolean.cpp:250-286)
+    const int *truncOcc;
     int *retriFace;  // [nTri - uncutA - uncutB] face of each re-triangulated triangle
     int8_t *label;
     unsigned int *counters;

@@ -315,11 +315,39 @@ __global__ void k_face_status(int nFaces, const int *__restrict__ faceSide, cons
         atomicMin(firstFail + faceSide[f], f);
 }
 
-__global__ void k_not_flag(int n, const int *__restrict__ flag, int *out)
+// 1 for the uncut triangles the reference keeps: not cut, and not past the mesh's truncation point
+__global__ void k_not_flag(int n, const int *__restrict__ flag, int *out, const int *__restrict__ truncOcc)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
-        out[i] = flag[i] ? 0 : 1;
+        out[i] = (flag[i] || i > *truncOcc / 3) ? 0 : 1;
+}
+
+// Truncation point of a mesh that holds a directed edge twice: every uncut triangle's edges in insertion
+// order (occurrence 3 i + k) into a table keeping the first occurrence of each half-edge; the first
+// occurrence that finds its half-edge already taken is where the reference's insertion fails.
+__global__ void k_trunc_insert(int nt, const uint32_t *__restrict__ t, const int *__restrict__ cut, uint64_t *keys,
+                               int *vals, uint32_t mask)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt || cut[i])
+        return;
+    for (int k = 0; k < 3; ++k)
+        u64map_insert_min(keys, vals, mask, he_key(t[3 * (size_t)i + k], t[3 * (size_t)i + (k + 1) % 3]), 3 * i + k);
+}
+
+__global__ void k_trunc_find(int nt, const uint32_t *__restrict__ t, const int *__restrict__ cut,
+                             const uint64_t *__restrict__ keys, const int *__restrict__ vals, uint32_t mask,
+                             int *truncOcc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt || cut[i])
+        return;
+    for (int k = 0; k < 3; ++k) {
+        const int occ = 3 * i + k;
+        if (u64map_find(keys, vals, mask, he_key(t[3 * (size_t)i + k], t[3 * (size_t)i + (k + 1) % 3])) < occ)
+            atomicMin(truncOcc, occ);
+    }
 }
 
 __global__ void k_tri_mesh(int nTri, int uncutA, int uncutB, int retriA, int8_t *triMesh, int8_t *isUncut)
@@ -355,7 +383,7 @@ struct sb_boolean {
     sb_options opts;
     cudaStream_t s = nullptr;
     // working and result buffers
-    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small;
+    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small, trunc;
     unsigned int candCap = 0;
     bool combined = false;
     sb_status status = SB_ERR_NOT_COMBINED;
@@ -450,6 +478,10 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemsetAsync(b->small.ptr, 0, 1024, s));
 
     const int nA = A.nt, nB = B.nt;
+    // directed edges held more than once per input mesh (1: unknown, treated as present)
+    int adjDup[2] = {1, 1};
+    int *d_truncOcc = reinterpret_cast<int *>(b->small.as<char>() + 640);
+    SB_CUDA_CHECK(cudaMemsetAsync(d_truncOcc, 0x7F, 2 * sizeof(int), s)); // no truncation
     // ---------------- broad phase ----------------
     if (b->candCap == 0)
         b->candCap = (unsigned int)std::max<size_t>(4096, 4 * ((size_t)nA + (size_t)nB));
@@ -467,6 +499,10 @@ sb_status combine_impl(sb_boolean *b)
         (void)o_sel;
         SB_CUDA_CHECK(cudaMemsetAsync(d_count, 0, sizeof(unsigned int), s));
         SB_CUDA_CHECK(cudaMemsetAsync(d_stats, 0, 8 * sizeof(unsigned long long), s));
+        if (attempt == 0 && A.adj && B.adj) { // read with the candidate count below
+            SB_CUDA_CHECK(cudaMemcpyAsync(adjDup, A.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SB_CUDA_CHECK(cudaMemcpyAsync(adjDup + 1, B.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
+        }
         launch_broad(fp64, A, B, reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw), d_count, b->candCap,
                      d_stats, s);
         SB_CUDA_CHECK(cudaGetLastError());
@@ -736,12 +772,28 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemsetAsync(g.cutA, 0, sizeof(int) * (nA + 1), s));
     SB_CUDA_CHECK(cudaMemsetAsync(g.cutB, 0, sizeof(int) * (nB + 1), s));
     launch_mark_cut(g, s);
+    g.truncOcc = d_truncOcc;
+    for (int side = 0; side < 2; ++side) {
+        // a mesh holding a directed edge twice: find where the reference's uncut-triangle insertion stops
+        const MeshDev &M = side == 0 ? A : B;
+        if (adjDup[side] == 0 || M.nt == 0)
+            continue;
+        const uint32_t cap = pow2_at_least(2 * 3 * (size_t)M.nt);
+        SB_CUDA_CHECK(b->trunc.ensure((sizeof(uint64_t) + sizeof(int)) * (size_t)cap));
+        uint64_t *tk = b->trunc.as<uint64_t>();
+        int *tv = reinterpret_cast<int *>(tk + cap);
+        SB_CUDA_CHECK(cudaMemsetAsync(tk, 0xFF, sizeof(uint64_t) * cap, s));
+        SB_CUDA_CHECK(cudaMemsetAsync(tv, 0x7F, sizeof(int) * cap, s));
+        const int *cutM = side == 0 ? g.cutA : g.cutB;
+        SB_COUNT(k_trunc_insert)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1);
+        SB_COUNT(k_trunc_find)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1, d_truncOcc + side);
+    }
     SB_CUDA_CHECK(cudaMemsetAsync(notA, 0, sizeof(int) * (nA + 1), s));
     SB_CUDA_CHECK(cudaMemsetAsync(notB, 0, sizeof(int) * (nB + 1), s));
     if (nA > 0)
-        SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA);
+        SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA, d_truncOcc);
     if (nB > 0)
-        SB_COUNT(k_not_flag)<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB);
+        SB_COUNT(k_not_flag)<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB, d_truncOcc + 1);
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, notA, g.uncutRankA, nA + 1, s);
     }));
@@ -758,11 +810,6 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 2, retriRank + FA, sizeof(int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 3, retriRank + nFaces, sizeof(int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaMemcpyAsync(firstFail, d_firstFail, sizeof firstFail, cudaMemcpyDeviceToHost, s));
-    int adjDup[2] = {1, 1}; // directed edges held twice in an input mesh (grouping then hashes every half-edge)
-    if (A.adj && B.adj) {
-        SB_CUDA_CHECK(cudaMemcpyAsync(adjDup, A.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaMemcpyAsync(adjDup + 1, B.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
-    }
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
     g.useAdj = adjDup[0] == 0 && adjDup[1] == 0;
     g.uncutA = cnts[0];
@@ -1331,7 +1378,7 @@ void sb_boolean_destroy(sb_boolean *b)
     if (!b)
         return;
     for (DevBuf *d : {&b->cand, &b->isect, &b->faces, &b->scratch, &b->cut, &b->weld, &b->arr, &b->groups, &b->res,
-                      &b->cub, &b->small})
+                      &b->cub, &b->small, &b->trunc})
         d->release();
     if (b->evInit)
         for (auto &e : b->ev)

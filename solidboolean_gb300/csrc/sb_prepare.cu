@@ -247,6 +247,8 @@ __global__ void k_adj_find(int nt, const uint32_t *__restrict__ t, const uint64_
     if (i >= nt)
         return;
     const uint32_t v[3] = {t[3 * (size_t)i], t[3 * (size_t)i + 1], t[3 * (size_t)i + 2]};
+    if (v[0] == v[1] && v[1] == v[2])
+        atomicAdd(adjDup, 1); // (a, a, a) holds the edge (a, a) three times
     for (int k = 0; k < 3; ++k) {
         const uint32_t a = v[k], b = v[(k + 1) % 3];
         if (u64map_find(keys, vals, mask, he_key(a, b)) != i)
