@@ -571,6 +571,19 @@ sb_status combine_impl(sb_boolean *b)
     int *uqA = (int *)(ib + o_uqA), *uqB = (int *)(ib + o_uqB), *ctA = (int *)(ib + o_ctA), *ctB = (int *)(ib + o_ctB);
     b->d_pairAB = pairAB;
     b->d_segK = segK;
+    // the leaf orders may still be building on the meshes' second streams (they overlap the broad and
+    // narrow phases); from here on the stream waits for them
+    for (const sb_mesh *cm : {b->first, b->second})
+        if (cm->rankPending && cm->aux)
+            SB_CUDA_CHECK(cudaStreamWaitEvent(s, cm->auxJoin, 0));
+    auto rankResults = [&]() -> sb_status {
+        for (const sb_mesh *cm : {b->first, b->second}) {
+            const sb_status r = reference_rank_result(const_cast<sb_mesh *>(cm));
+            if (r != SB_OK)
+                return r;
+        }
+        return SB_OK;
+    };
     const bool useRank = b->opts.order == SB_ORDER_REFERENCE && A.rankValid && B.rankValid;
     int FA = 0, FB = 0;
     if (K > 0) {
@@ -607,6 +620,12 @@ sb_status combine_impl(sb_boolean *b)
             return r;
         FA = (int)runs[0];
         FB = (int)runs[1];
+    }
+    {
+        // synchronised past the leaf orders (when there were pairs to group; else at the end)
+        const sb_status r = K > 0 ? rankResults() : SB_OK;
+        if (r != SB_OK)
+            return r;
     }
     const int nFaces = FA + FB;
     st.cut_faces_first = FA;
@@ -953,6 +972,11 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaMemcpyAsync(counters, d_counters, sizeof counters, cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
     SB_CUDA_CHECK(cudaGetLastError());
+    {
+        const sb_status r = rankResults();
+        if (r != SB_OK)
+            return r;
+    }
     st.box_tests = dstats[0];
     st.box_fallbacks = dstats[1];
     st.sign_tests = dstats[2];
@@ -1178,6 +1202,10 @@ void sb_mesh_destroy(sb_mesh *m)
     m->buf.release();
     m->tmp.release();
     m->rankTmp.release();
+    if (m->rankPending && m->aux)
+        cudaStreamSynchronize(m->aux);
+    if (m->rankCheck)
+        cudaFreeHost(m->rankCheck);
     if (m->aux)
         cudaStreamDestroy(m->aux);
     if (m->auxFork)
@@ -1225,8 +1253,8 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
             SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->s));
             SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
             sb_status rb = SB_OK;
-            std::thread helper([&]() { rb = prepare_mesh(mb, b->opts.order, b->side); });
-            sb_status ra = prepare_mesh(ma, b->opts.order, b->s);
+            std::thread helper([&]() { rb = prepare_mesh(mb, b->opts.order, b->side, false); });
+            sb_status ra = prepare_mesh(ma, b->opts.order, b->s, false);
             helper.join();
             if (ra != SB_OK)
                 return ra;
@@ -1237,7 +1265,7 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
         }
         for (sb_mesh *m : {ma, mb})
             if (!m->prepared) {
-                sb_status r = prepare_mesh(m, b->opts.order, b->s);
+                sb_status r = prepare_mesh(m, b->opts.order, b->s, false);
                 if (r != SB_OK)
                     return r;
             }

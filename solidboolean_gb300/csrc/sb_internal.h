@@ -71,6 +71,8 @@ struct sb_mesh {
     cudaEvent_t auxFork = nullptr, auxJoin = nullptr;
     bool prepared = false;
     bool adjValid = false;         // adj / adjDup computed for the current triangles
+    int *rankCheck = nullptr;      // pinned: the leaf-order build's counters, read once its stream is done
+    bool rankPending = false;      // rankCheck not yet read (build_reference_rank without waiting)
     bool ownsInput = true;
     cudaStream_t stream = nullptr;
     std::vector<double> hostV;    // only for host-created meshes (kept for re-preparation)
@@ -79,7 +81,10 @@ struct sb_mesh {
 
 namespace sbg {
 // sb_prepare.cu
-sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s);
+// With waitRank false the reference leaf order may still be running on m->aux when this returns: the caller
+// orders later work after m->auxJoin and calls reference_rank_result after a synchronisation past it.
+sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank = true);
 // sb_refrank.cu: position of each triangle in the reference tree's leaf order
-sb_status build_reference_rank(sb_mesh *m, cudaStream_t s);
+sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait);
+sb_status reference_rank_result(sb_mesh *m);
 } // namespace sbg

@@ -257,7 +257,7 @@ __global__ void k_adj_find(int nt, const uint32_t *__restrict__ t, const uint64_
     }
 }
 
-sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
+sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank)
 {
     MeshDev &d = m->d;
     const int nt = d.nt;
@@ -374,9 +374,10 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s)
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = false;
     if (fork) {
-        sb_status st = build_reference_rank(m, m->aux); // returns once its own stream has finished
+        sb_status st = build_reference_rank(m, m->aux, waitRank);
         SB_CUDA_CHECK(cudaEventRecord(m->auxJoin, m->aux));
-        SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
+        if (waitRank)
+            SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
         if (st != SB_OK)
             return st;
     }

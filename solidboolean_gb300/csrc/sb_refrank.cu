@@ -1275,7 +1275,41 @@ static int top_grid(int nt)
     return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 2)));
 }
 
-sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
+// Status of a leaf-order build from its counters and barrier record (12 ints).
+static sb_status rank_status(const int *chk)
+{
+    const int *cnt = chk;
+    if (chk[kCtCount + 2]) { // GridBar::err
+        set_last_error("reference tree: a grid barrier timed out");
+        return SB_ERR_CUDA;
+    }
+    if (cnt[kCtOverflow]) {
+        set_last_error("reference tree node capacity exceeded");
+        return SB_ERR_CAPACITY;
+    }
+    if (cnt[kCtFirst] < cnt[kCtLast]) {
+        set_last_error("reference tree deeper than the level limit");
+        return SB_ERR_CAPACITY;
+    }
+    if (cnt[kCtSubErr]) {
+        set_last_error("reference tree: a subtree exceeded its node records");
+        return SB_ERR_CAPACITY;
+    }
+    return SB_OK;
+}
+
+sb_status reference_rank_result(sb_mesh *m)
+{
+    if (!m->rankPending)
+        return SB_OK;
+    m->rankPending = false;
+    const sb_status st = rank_status(m->rankCheck);
+    if (st != SB_OK)
+        m->d.rankValid = false;
+    return st;
+}
+
+sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
 {
     MeshDev &d = m->d;
     const int nt = d.nt;
@@ -1338,30 +1372,19 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s)
         SB_COUNT(k_rr_subtree)<<<maxNodes, kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri,
                                                                         scg, d.rank, counters);
     }
-    int cnt[kCtCount];
-    GridBar hb;
-    SB_CUDA_CHECK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(&hb, bar, sizeof hb, cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaStreamSynchronize(s));
-    if (hb.err) {
-        set_last_error("reference tree: a grid barrier timed out");
-        return SB_ERR_CUDA;
-    }
-    if (cnt[kCtOverflow]) {
-        set_last_error("reference tree node capacity exceeded");
-        return SB_ERR_CAPACITY;
-    }
-    if (cnt[kCtFirst] < cnt[kCtLast]) {
-        set_last_error("reference tree deeper than the level limit");
-        return SB_ERR_CAPACITY;
-    }
-    if (cnt[kCtSubErr]) {
-        set_last_error("reference tree: a subtree exceeded its node records");
-        return SB_ERR_CAPACITY;
-    }
+    // counters and barrier record to pinned host memory; read now, or by reference_rank_result once the
+    // caller has synchronised past this stream
+    if (!m->rankCheck)
+        SB_CUDA_CHECK(cudaMallocHost((void **)&m->rankCheck, 16 * sizeof(int)));
+    SB_CUDA_CHECK(cudaMemcpyAsync(m->rankCheck, counters, kCtCount * sizeof(int), cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaMemcpyAsync(m->rankCheck + kCtCount, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaGetLastError());
     d.rankValid = true;
-    return SB_OK;
+    m->rankPending = true;
+    if (!wait)
+        return SB_OK;
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    return reference_rank_result(m);
 }
 
 } // namespace sbg
