@@ -12,6 +12,8 @@
 //   sides             decideGroupSide / isPointInMesh (:482-510, 48-92): three axis rays from the centroid
 //                     of each region's representative triangle, hit points deduplicated by PositionKey,
 //                     inside when at least two of the three parities are odd
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "sb_assemble.cuh"
@@ -408,39 +410,30 @@ __global__ void k_region_list(int nTri, const int *__restrict__ root, const int 
 // (FP32 boxes rounded outward, or exact FP64 boxes in the plain form), test reached triangles exactly in
 // FP64 (closed-interval box test, plane hit, three same-sign normals) and collect the hit points; the
 // parity of the number of distinct PositionKeys decides the axis.
-constexpr int kSideWarps = 4;
-constexpr int kSideStack = 1536; // per warp; 4 warps x (1536 x 4 B + 128 x 24 B) = 36 KB of static smem
-constexpr int kSideHits = 128;
-
-template <bool FP64>
-__global__ void __launch_bounds__(32 * kSideWarps)
-    k_sides(unsigned int nReps, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
-            const uint32_t *__restrict__ newT, const double *__restrict__ newV, const int8_t *__restrict__ triMesh,
-            MeshDev A, MeshDev B, double factor, int *insideCount, unsigned int *errors)
-{
-    __shared__ int stack[kSideWarps][kSideStack];
-    __shared__ Key hits[kSideWarps][kSideHits];
-    __shared__ int spS[kSideWarps], nhS[kSideWarps], errS[kSideWarps];
-    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned full = 0xFFFFFFFFu;
-    unsigned int w = blockIdx.x * kSideWarps + wl;
-    if (w >= 3 * nReps)
-        return;
-    const int r = reps[w / 3];
-    const int axis = (int)(w % 3);
-    const int rep = repOfRoot[r];
-    const MeshDev &M = triMesh[rep] == 0 ? B : A; // the other mesh
-    const uint32_t *tv = newT + 3 * (size_t)rep;
-    d3 v0 = mk(newV[3 * (size_t)tv[0]], newV[3 * (size_t)tv[0] + 1], newV[3 * (size_t)tv[0] + 2]);
-    d3 v1 = mk(newV[3 * (size_t)tv[1]], newV[3 * (size_t)tv[1] + 1], newV[3 * (size_t)tv[1] + 2]);
-    d3 v2 = mk(newV[3 * (size_t)tv[2]], newV[3 * (size_t)tv[2] + 1], newV[3 * (size_t)tv[2] + 2]);
-    const d3 p = divs((v0 + v1) + v2, 3.0);
-    const d3 ax = mk(axis == 0 ? kDblMax : kDblEps, axis == 1 ? kDblMax : kDblEps, axis == 2 ? kDblMax : kDblEps);
-    const d3 e = p + ax;
+// One axis ray of a region's representative triangle (src/solidboolean.cpp:482-510, 48-92): from the
+// triangle's centroid p to e = p + (DBL_MAX on the axis, DBL_EPSILON on the others), its query box as the
+// reference's tree query builds it (update with p then e), and the FP32 box rounded outward.
+struct SideRay {
+    d3 p, u;
     double qlo[3], qhi[3];
     float olo[3], ohi[3];
+    int target; // mesh whose triangles the ray tests (the other mesh): 0 first, 1 second
+    int region;
+};
+
+__device__ SideRay side_ray(int rep, int axis, int region, const uint32_t *__restrict__ newT,
+                            const double *__restrict__ newV, const int8_t *__restrict__ triMesh)
+{
+    SideRay r;
+    const uint32_t *tv = newT + 3 * (size_t)rep;
+    const d3 v0 = mk(newV[3 * (size_t)tv[0]], newV[3 * (size_t)tv[0] + 1], newV[3 * (size_t)tv[0] + 2]);
+    const d3 v1 = mk(newV[3 * (size_t)tv[1]], newV[3 * (size_t)tv[1] + 1], newV[3 * (size_t)tv[1] + 2]);
+    const d3 v2 = mk(newV[3 * (size_t)tv[2]], newV[3 * (size_t)tv[2] + 1], newV[3 * (size_t)tv[2] + 2]);
+    r.p = divs((v0 + v1) + v2, 3.0);
+    const d3 ax = mk(axis == 0 ? kDblMax : kDblEps, axis == 1 ? kDblMax : kDblEps, axis == 2 ? kDblMax : kDblEps);
+    const d3 e = r.p + ax;
     for (int k = 0; k < 3; ++k) {
-        double a = comp(p, k), b = comp(e, k);
+        const double a = comp(r.p, k), b = comp(e, k);
         double lo = kDblMax, hi = -kDblMax; // AxisAlignedBoudingBox::update with p then e
         if (a > hi)
             hi = a;
@@ -450,129 +443,269 @@ __global__ void __launch_bounds__(32 * kSideWarps)
             hi = b;
         if (b < lo)
             lo = b;
-        qlo[k] = lo;
-        qhi[k] = hi;
-        olo[k] = __double2float_rd(lo);
-        ohi[k] = __double2float_ru(hi);
+        r.qlo[k] = lo;
+        r.qhi[k] = hi;
+        r.olo[k] = __double2float_rd(lo);
+        r.ohi[k] = __double2float_ru(hi);
     }
-    const d3 u = e - p;
-    if (lane == 0) {
-        spS[wl] = 0;
-        nhS[wl] = 0;
-        errS[wl] = 0;
+    r.u = e - r.p;
+    r.target = triMesh[rep] == 0 ? 1 : 0;
+    r.region = region;
+    return r;
+}
+
+// The reference's test of one triangle against the ray: box overlap in FP64, then the segment-plane
+// intersection and the point-in-triangle test by normals. Writes the hit's PositionKey.
+__device__ bool side_hit(const MeshDev &M, int ti, const SideRay &ray, double factor, Key &key)
+{
+    const double *bx = M.box64 + 6 * (size_t)ti;
+    for (int k = 0; k < 3; ++k)
+        if (!(bx[k] <= ray.qhi[k] && bx[3 + k] >= ray.qlo[k]))
+            return false;
+    const uint32_t *t = M.t + 3 * (size_t)ti;
+    d3 tp[3];
+    for (int k = 0; k < 3; ++k)
+        tp[k] = mk(M.v[3 * (size_t)t[k]], M.v[3 * (size_t)t[k] + 1], M.v[3 * (size_t)t[k] + 2]);
+    const d3 n = unit_normal(tp[0], tp[1], tp[2]);
+    const d3 wv = ray.p - tp[0];
+    const double d = dot(n, ray.u);
+    const double nn = dot(neg(n), wv);
+    if (fabs(d) <= kDblEps)
+        return false;
+    const double s = nn / d;
+    if (s < 0 || s > 1 || isnan(s) || isinf(s))
+        return false;
+    const d3 x = ray.p + scale(s, ray.u);
+    const d3 n0 = unit_normal(x, tp[0], tp[1]);
+    const d3 n1 = unit_normal(x, tp[1], tp[2]);
+    const d3 n2 = unit_normal(x, tp[2], tp[0]);
+    if (!(dot(n0, n1) > 0 && dot(n0, n2) > 0))
+        return false;
+    key = make_key(x, factor);
+    return true;
+}
+
+constexpr int kSideHits = 128; // hit keys kept per ray (more sets the side-error counter)
+
+__device__ __forceinline__ void side_record(const SideRay &ray, int rayId, const MeshDev &M, int ti, double factor,
+                                            Key *hits, int *hitCount, unsigned int *errors)
+{
+    Key key;
+    if (!side_hit(M, ti, ray, factor, key))
+        return;
+    const int slot = atomicAdd(hitCount + rayId, 1);
+    if (slot < kSideHits)
+        hits[(size_t)rayId * kSideHits + slot] = key;
+    else
+        atomicAdd(errors, 1u);
+}
+
+
+// Few rays: every triangle of the target mesh against all rays, one thread per triangle (the triangle's box
+// read once, the rays from shared memory), instead of one latency-bound tree walk per ray. The FP32 box
+// against the outward-rounded query is conservative; side_hit then applies the reference's FP64 box test.
+constexpr int kBruteRays = 96;
+
+__global__ void k_side_rays(int nRays, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
+                            const uint32_t *__restrict__ newT, const double *__restrict__ newV,
+                            const int8_t *__restrict__ triMesh, SideRay *rays, int *hitCount)
+{
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nRays)
+        return;
+    const int r = reps[w / 3];
+    rays[w] = side_ray(repOfRoot[r], w % 3, r, newT, newV, triMesh);
+    hitCount[w] = 0;
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(256) k_side_brute(int target, MeshDev M, int nRays, const SideRay *__restrict__ rays,
+                                                    double factor, Key *hits, int *hitCount, unsigned int *errors)
+{
+    __shared__ SideRay sr[kBruteRays];
+    __shared__ int ids[kBruteRays], nMine;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int k = 0; k < nRays; ++k)
+            if (rays[k].target == target)
+                ids[c++] = k;
+        nMine = c;
     }
-    __syncwarp();
-    auto test_tri = [&](int ti) {
-        const double *bx = M.box64 + 6 * (size_t)ti;
-        for (int k = 0; k < 3; ++k)
-            if (!(bx[k] <= qhi[k] && bx[3 + k] >= qlo[k]))
-                return;
-        const uint32_t *t = M.t + 3 * (size_t)ti;
-        d3 tp[3];
-        for (int k = 0; k < 3; ++k)
-            tp[k] = mk(M.v[3 * (size_t)t[k]], M.v[3 * (size_t)t[k] + 1], M.v[3 * (size_t)t[k] + 2]);
-        d3 n = unit_normal(tp[0], tp[1], tp[2]);
-        d3 wv = p - tp[0];
-        double d = dot(n, u);
-        double nn = dot(neg(n), wv);
-        if (fabs(d) <= kDblEps)
-            return;
-        double s = nn / d;
-        if (s < 0 || s > 1 || isnan(s) || isinf(s))
-            return;
-        d3 x = p + scale(s, u);
-        d3 n0 = unit_normal(x, tp[0], tp[1]);
-        d3 n1 = unit_normal(x, tp[1], tp[2]);
-        d3 n2 = unit_normal(x, tp[2], tp[0]);
-        if (!(dot(n0, n1) > 0 && dot(n0, n2) > 0))
-            return;
-        int k = atomicAdd(&nhS[wl], 1);
-        if (k < kSideHits)
-            hits[wl][k] = make_key(x, factor);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nMine; k += blockDim.x)
+        sr[k] = rays[ids[k]];
+    __syncthreads();
+    const int n = nMine;
+    for (int ti = blockIdx.x * blockDim.x + threadIdx.x; ti < M.nt; ti += gridDim.x * blockDim.x) {
+        float b32[6];
+        double b64[6];
+        if (FP64)
+            for (int k = 0; k < 6; ++k)
+                b64[k] = M.box64[6 * (size_t)ti + k];
         else
-            errS[wl] = 1;
-    };
-    if (M.nt > 0) {
-        if (M.root < 0) {
-            if (lane == 0)
-                test_tri(M.leafTri[0]);
-        } else if (lane == 0) {
-            stack[wl][0] = M.root;
-            spS[wl] = 1;
-        }
-        __syncwarp();
-        for (int iter = 0; iter < (1 << 20); ++iter) {
-            int sp = spS[wl];
-            int n = min(sp, 32);
-            if (n == 0)
-                break;
-            int node = lane < n ? stack[wl][sp - n + lane] : -1;
-            __syncwarp();
-            int push[2] = {-1, -1};
-            if (node >= 0) {
-                int2 ch = M.child[node];
-                int cs[2] = {ch.x, ch.y};
-                for (int k = 0; k < 2; ++k) {
-                    int c = cs[k];
-                    if (c < 0) {
-                        test_tri(M.leafTri[~c]);
-                        continue;
-                    }
-                    bool hit;
-                    if (FP64) {
-                        const double *bx = M.nbox64 + 6 * (size_t)c;
-                        hit = qlo[0] <= bx[3] && qhi[0] >= bx[0] && qlo[1] <= bx[4] && qhi[1] >= bx[1] &&
-                              qlo[2] <= bx[5] && qhi[2] >= bx[2];
-                    } else {
-                        const float *bx = M.nbox32 + 6 * (size_t)c;
-                        hit = olo[0] <= bx[3] && ohi[0] >= bx[0] && olo[1] <= bx[4] && ohi[1] >= bx[1] &&
-                              olo[2] <= bx[5] && ohi[2] >= bx[2];
-                    }
-                    if (hit)
-                        push[k] = c;
-                }
-            }
-            int cnt = (push[0] >= 0) + (push[1] >= 0);
-            int incl = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-                int v = __shfl_up_sync(full, incl, o);
-                if (lane >= o)
-                    incl += v;
-            }
-            int total = __shfl_sync(full, incl, 31);
-            int base = sp - n;
-            if (base + total > kSideStack) {
-                if (lane == 0)
-                    errS[wl] = 1;
-                break;
-            }
-            int pos = base + incl - cnt;
-            for (int k = 0; k < 2; ++k)
-                if (push[k] >= 0)
-                    stack[wl][pos++] = push[k];
-            __syncwarp();
-            if (lane == 0)
-                spS[wl] = base + total;
-            __syncwarp();
+            for (int k = 0; k < 6; ++k)
+                b32[k] = M.box32[6 * (size_t)ti + k];
+        for (int k = 0; k < n; ++k) {
+            const SideRay &ray = sr[k];
+            bool over = true;
+            for (int a = 0; a < 3; ++a)
+                over = over && (FP64 ? (b64[a] <= ray.qhi[a] && b64[3 + a] >= ray.qlo[a])
+                                     : (b32[a] <= ray.ohi[a] && b32[3 + a] >= ray.olo[a]));
+            if (!over)
+                continue;
+            Key key;
+            if (!side_hit(M, ti, ray, factor, key))
+                continue;
+            const int id = ids[k];
+            const int slot = atomicAdd(hitCount + id, 1);
+            if (slot < kSideHits)
+                hits[(size_t)id * kSideHits + slot] = key;
+            else
+                atomicAdd(errors, 1u);
         }
     }
-    __syncwarp();
-    // distinct keys among the hits (std::set<PositionKey> in the reference)
-    int nh = min(nhS[wl], kSideHits);
+}
+
+// the exact test of the listed (ray, triangle) pairs, one per thread
+__global__ void k_side_pairs(const int *__restrict__ pairCount, int pairCap, const int2 *__restrict__ pairs,
+                             const SideRay *__restrict__ rays, MeshDev A, MeshDev B, double factor, Key *hits,
+                             int *hitCount, unsigned int *errors)
+{
+    const int n = min(*pairCount, pairCap);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int2 pr = pairs[q];
+        const SideRay ray = rays[pr.x];
+        side_record(ray, pr.x, ray.target == 0 ? A : B, pr.y, factor, hits, hitCount, errors);
+    }
+}
+
+// one warp per ray: distinct hit keys (the reference's std::set<PositionKey>), odd count = inside
+__global__ void k_side_parity(int nRays, const SideRay *__restrict__ rays, const Key *__restrict__ hits,
+                              const int *__restrict__ hitCount, int *insideCount)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nRays)
+        return;
+    const Key *h = hits + (size_t)w * kSideHits;
+    const int nh = min(hitCount[w], kSideHits);
     int distinct = 0;
-    for (int h = lane; h < nh; h += 32) {
+    for (int i = lane; i < nh; i += 32) {
         bool dup = false;
-        for (int j = 0; j < h && !dup; ++j)
-            dup = key_eq(hits[wl][j], hits[wl][h]);
+        for (int j = 0; j < i && !dup; ++j)
+            dup = key_eq(h[j], h[i]);
         distinct += dup ? 0 : 1;
     }
     for (int o = 16; o > 0; o >>= 1)
-        distinct += __shfl_xor_sync(full, distinct, o);
+        distinct += __shfl_xor_sync(0xFFFFFFFFu, distinct, o);
+    if (lane == 0 && distinct % 2 != 0)
+        atomicAdd(insideCount + rays[w].region, 1);
+}
+
+// Many rays: one warp per ray walks the other mesh's LBVH (a node stack in shared memory, up to 32 nodes per
+// step) with the query box, FP32 node boxes and FP32 leaf boxes rounded conservatively (FP64 boxes in the
+// plain FP64 form), and lists the leaves that pass as (ray, triangle) pairs; the exact test then runs one pair
+// per lane in k_side_pairs. Pairs beyond the list's capacity are tested in place.
+constexpr int kTreeWarps = 4;
+constexpr int kSideStack = 1536; // nodes per warp
+
+template <bool FP64>
+__global__ void __launch_bounds__(32 * kTreeWarps)
+    k_tree_rays(int nRays, const SideRay *__restrict__ rays, MeshDev A, MeshDev B, double factor, Key *hits,
+                int *hitCount, unsigned int *errors, int2 *pairs, int *pairCount, int pairCap)
+{
+    __shared__ int stack[kTreeWarps][kSideStack];
+    __shared__ int spS[kTreeWarps];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xFFFFFFFFu;
+    const int w = blockIdx.x * kTreeWarps + wl;
+    if (w >= nRays)
+        return;
+    const SideRay ray = rays[w];
+    const MeshDev &M = ray.target == 0 ? A : B;
+    if (M.nt <= 0)
+        return;
+    auto leaf = [&](int ti) {
+        bool over = true;
+        for (int k = 0; k < 3; ++k) {
+            if (FP64) {
+                const double *bx = M.box64 + 6 * (size_t)ti;
+                over = over && bx[k] <= ray.qhi[k] && bx[3 + k] >= ray.qlo[k];
+            } else {
+                const float *bx = M.box32 + 6 * (size_t)ti;
+                over = over && bx[k] <= ray.ohi[k] && bx[3 + k] >= ray.olo[k];
+            }
+        }
+        if (!over)
+            return;
+        const int slot = atomicAdd(pairCount, 1);
+        if (slot < pairCap)
+            pairs[slot] = make_int2(w, ti);
+        else
+            side_record(ray, w, M, ti, factor, hits, hitCount, errors);
+    };
+    if (M.root < 0) {
+        if (lane == 0)
+            leaf(M.leafTri[0]);
+        return;
+    }
     if (lane == 0) {
-        if (errS[wl])
-            atomicAdd(errors, 1u);
-        if (distinct % 2 != 0)
-            atomicAdd(insideCount + r, 1);
+        stack[wl][0] = M.root;
+        spS[wl] = 1;
+    }
+    __syncwarp();
+    for (int iter = 0; iter < (1 << 20); ++iter) {
+        const int sp = spS[wl];
+        const int n = min(sp, 32);
+        if (n == 0)
+            break;
+        const int node = lane < n ? stack[wl][sp - n + lane] : -1;
+        __syncwarp();
+        int push[2] = {-1, -1};
+        if (node >= 0) {
+            const int2 ch = M.child[node];
+            const int cs[2] = {ch.x, ch.y};
+            for (int k = 0; k < 2; ++k) {
+                const int c = cs[k];
+                if (c < 0) {
+                    leaf(M.leafTri[~c]);
+                    continue;
+                }
+                bool hit;
+                if (FP64) {
+                    const double *bx = M.nbox64 + 6 * (size_t)c;
+                    hit = ray.qlo[0] <= bx[3] && ray.qhi[0] >= bx[0] && ray.qlo[1] <= bx[4] && ray.qhi[1] >= bx[1] &&
+                          ray.qlo[2] <= bx[5] && ray.qhi[2] >= bx[2];
+                } else {
+                    const float *bx = M.nbox32 + 6 * (size_t)c;
+                    hit = ray.olo[0] <= bx[3] && ray.ohi[0] >= bx[0] && ray.olo[1] <= bx[4] && ray.ohi[1] >= bx[1] &&
+                          ray.olo[2] <= bx[5] && ray.ohi[2] >= bx[2];
+                }
+                if (hit)
+                    push[k] = c;
+            }
+        }
+        const int cnt = (push[0] >= 0) + (push[1] >= 0);
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(full, incl, o);
+            if (lane >= o)
+                incl += v;
+        }
+        const int total = __shfl_sync(full, incl, 31);
+        const int base = sp - n;
+        if (base + total > kSideStack) {
+            if (lane == 0)
+                atomicAdd(errors, 1u);
+            break;
+        }
+        int pos = base + incl - cnt;
+        for (int k = 0; k < 2; ++k)
+            if (push[k] >= 0)
+                stack[wl][pos++] = push[k];
+        __syncwarp();
+        if (lane == 0)
+            spS[wl] = base + total;
+        __syncwarp();
     }
 }
 
@@ -760,19 +893,67 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
     }
 }
 
+constexpr int kPairsPerRay = 64; // pair-list capacity per ray (more are tested in place)
+
+size_t side_layout(AsmArgs &g, int nRays, char *base)
+{
+    Carve c;
+    const size_t n = (size_t)std::max(nRays, 1);
+    const size_t oRays = c.take<SideRay>(n), oHits = c.take<Key>(n * kSideHits), oCnt = c.take<int>(n + 1);
+    const size_t oPairs = c.take<int2>(kPairsPerRay * n);
+    if (base) {
+        g.sideRays = base + oRays;
+        g.sideHits = base + oHits;
+        g.sideHitCount = reinterpret_cast<int *>(base + oCnt);
+        g.sidePairs = base + oPairs;
+        g.sidePairCap = (int)(kPairsPerRay * n);
+    }
+    return c.off;
+}
+
 void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s)
 {
+    const int nRays = 3 * (int)nReps;
     if (nReps > 0) {
         KTime kt("k_sides", s);
-        count_launch();
-        if (fp64)
-            k_sides<true><<<nb(3 * (size_t)nReps, kSideWarps), 32 * kSideWarps, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
-                                                                   g.triMesh, g.A, g.B, g.factor, g.insideCount,
-                                                                   g.counters + kCntSideErrors);
-        else
-            k_sides<false><<<nb(3 * (size_t)nReps, kSideWarps), 32 * kSideWarps, 0, s>>>(nReps, g.reps, g.repOfRoot, g.newT, g.newV,
-                                                                    g.triMesh, g.A, g.B, g.factor, g.insideCount,
-                                                                    g.counters + kCntSideErrors);
+        SideRay *rays = reinterpret_cast<SideRay *>(g.sideRays);
+        Key *hits = reinterpret_cast<Key *>(g.sideHits);
+        int *pairCount = g.sideHitCount + nRays; // one past the per-ray counts
+        cudaMemsetAsync(pairCount, 0, sizeof(int), s);
+        SB_COUNT(k_side_rays)<<<nb(nRays, 128), 128, 0, s>>>(nRays, g.reps, g.repOfRoot, g.newT, g.newV, g.triMesh,
+                                                             rays, g.sideHitCount);
+        if (nRays <= kBruteRays) {
+            // few rays: every triangle against all of them
+            for (int target = 0; target < 2; ++target) {
+                const MeshDev &M = target == 0 ? g.A : g.B;
+                if (M.nt <= 0)
+                    continue;
+                const int grid = std::min(nb(M.nt, 256), 152 * 8);
+                count_launch();
+                if (fp64)
+                    k_side_brute<true><<<grid, 256, 0, s>>>(target, M, nRays, rays, g.factor, hits, g.sideHitCount,
+                                                            g.counters + kCntSideErrors);
+                else
+                    k_side_brute<false><<<grid, 256, 0, s>>>(target, M, nRays, rays, g.factor, hits, g.sideHitCount,
+                                                             g.counters + kCntSideErrors);
+            }
+        } else {
+            int2 *pairs = reinterpret_cast<int2 *>(g.sidePairs);
+            count_launch();
+            if (fp64)
+                k_tree_rays<true><<<nb(nRays, kTreeWarps), 32 * kTreeWarps, 0, s>>>(
+                    nRays, rays, g.A, g.B, g.factor, hits, g.sideHitCount, g.counters + kCntSideErrors, pairs,
+                    pairCount, g.sidePairCap);
+            else
+                k_tree_rays<false><<<nb(nRays, kTreeWarps), 32 * kTreeWarps, 0, s>>>(
+                    nRays, rays, g.A, g.B, g.factor, hits, g.sideHitCount, g.counters + kCntSideErrors, pairs,
+                    pairCount, g.sidePairCap);
+            SB_COUNT(k_side_pairs)<<<nb(g.sidePairCap, 128), 128, 0, s>>>(pairCount, g.sidePairCap, pairs, rays, g.A,
+                                                                          g.B, g.factor, hits, g.sideHitCount,
+                                                                          g.counters + kCntSideErrors);
+        }
+        SB_COUNT(k_side_parity)<<<nb(32 * (size_t)nRays, 128), 128, 0, s>>>(nRays, rays, hits, g.sideHitCount,
+                                                                            g.insideCount);
     }
     if (g.nTri > 0)
         {

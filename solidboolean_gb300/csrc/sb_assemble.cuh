@@ -60,6 +60,10 @@ struct AsmArgs {
     int *retriFace;  // [nTri - uncutA - uncutB] face of each re-triangulated triangle
     int8_t *label;
     unsigned int *counters;
+    // side rays: per ray its setup, hit keys and hit count, and the (ray, triangle) pairs for the exact test
+    void *sideRays, *sideHits, *sidePairs;
+    int *sideHitCount; // nRays + 1: the last one counts the pairs
+    int sidePairCap;
 };
 
 void launch_weld(const AsmArgs &g, cudaStream_t s);
@@ -69,6 +73,8 @@ void launch_arrangement(const AsmArgs &g, cudaStream_t s);
 void launch_loops(const AsmArgs &g, cudaStream_t s);
 void launch_groups(const AsmArgs &g, cudaStream_t s);
 void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s);
+// layout of the side-ray buffers for nRays rays (base null: bytes only)
+size_t side_layout(AsmArgs &g, int nRays, char *base);
 void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s);
 void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s);
 

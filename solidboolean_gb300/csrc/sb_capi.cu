@@ -383,7 +383,7 @@ struct sb_boolean {
     sb_options opts;
     cudaStream_t s = nullptr;
     // working and result buffers
-    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small, trunc;
+    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small, trunc, sides;
     unsigned int candCap = 0;
     bool combined = false;
     sb_status status = SB_ERR_NOT_COMBINED;
@@ -886,6 +886,7 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_par = cg2.take<int>(nTri + 1), o_sf = cg2.take<int>(nTri + 1), o_smn = cg2.take<int>(nTri + 1);
     size_t o_rmn = cg2.take<int>(nTri + 1), o_ror = cg2.take<int>(nTri + 1), o_rep = cg2.take<int>(nTri + 1);
     size_t o_ins = cg2.take<int>(nTri + 1);
+
     SB_CUDA_CHECK(b->groups.ensure(cg2.off));
     char *gb = b->groups.as<char>();
     g.edgeKeys = (uint64_t *)(gb + o_ek);
@@ -904,6 +905,7 @@ sb_status combine_impl(sb_boolean *b)
     g.repOfRoot = (int *)(gb + o_ror);
     g.reps = (int *)(gb + o_rep);
     g.insideCount = (int *)(gb + o_ins);
+
     SB_COUNT(k_fill_u64)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeKeys, kEmpty64);
     SB_COUNT(k_fill_i32)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeVals, INT_MAX);
     SB_CUDA_CHECK(cudaMemsetAsync(g.degree, 0, sizeof(int) * (nNew + 1), s));
@@ -929,6 +931,8 @@ sb_status combine_impl(sb_boolean *b)
             return r;
     }
     const unsigned int nReps = counters[kCntReps];
+    SB_CUDA_CHECK(b->sides.ensure(side_layout(g, 3 * (int)nReps, nullptr)));
+    side_layout(g, 3 * (int)nReps, b->sides.as<char>());
     launch_sides(g, nReps, fp64, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[6], s));
@@ -1406,7 +1410,7 @@ void sb_boolean_destroy(sb_boolean *b)
     if (!b)
         return;
     for (DevBuf *d : {&b->cand, &b->isect, &b->faces, &b->scratch, &b->cut, &b->weld, &b->arr, &b->groups, &b->res,
-                      &b->cub, &b->small, &b->trunc})
+                      &b->cub, &b->small, &b->trunc, &b->sides})
         d->release();
     if (b->evInit)
         for (auto &e : b->ev)
