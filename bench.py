@@ -185,6 +185,12 @@ def kernel_bytes(name: str, st: dict, na: int, nb: int, nva: int, nvb: int) -> f
     }.get(name, 0.0)
 
 
+# DRAM bytes per launch (read + write) of the kernels captured with ncu on this workload; the figures and
+# the command are in profiles/kernels_pair_large_L7.txt
+MEASURED_TRAFFIC = {"k_rr_top": 32.85e6, "k_rr_subtree": 35.55e6, "k_faces": 14.53e6, "k_broad": 19.56e6,
+                    "k_union": 26.97e6}
+
+
 def rr_levels(n: int) -> int:
     """levels of the reference tree's large-node phase for n triangles (nodes above 1024 members split)"""
     levels = 1
@@ -341,7 +347,7 @@ def gpu_arm(args, rank, world, local, dist):
         ach = alg / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
         roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 5), "peak_kind": peak_kind, "avg_launch_ms": round(avg_ms, 4),
-                "algorithmic_bytes": alg, "traffic": None,
+                "algorithmic_bytes": alg, "traffic": MEASURED_TRAFFIC.get(name),
                 "share_of_step": round(tot_ms / max(sum(t32), 1e-9), 4)}
     per_kernel = {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 4), "launches": v[1]} for k, v in kern.items()}
     return {
