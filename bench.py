@@ -336,6 +336,22 @@ def gpu_arm(args, rank, world, local, dist):
     total_pairs = allsum(dist, float(C))
     value = total_pairs / (ms32_max / 1e3)
     e2e_s = allmax(dist, statistics.mean(e2e_times))
+
+    # batched workload: independent pairs of mixed subdivision levels through sb_batch_combine, host inputs,
+    # statuses only (the per-pair results stay on the device side of each worker); wall time of the call
+    batch = None
+    if args.batch_pairs > 0:
+        pairs = mg.batch(args.batch_pairs, SEED, 5)
+        sbg.batch_combine(pairs[:64], workers=8, keep=False)  # warm-up: handles, streams, buffers
+        t0 = time.perf_counter()
+        statuses, _ = sbg.batch_combine(pairs, workers=8, keep=False)
+        t1 = time.perf_counter()
+        batch = {"workload": f"{args.batch_pairs} pairs: icospheres of levels U{{1..5}}, scale U[0.5, 2], random "
+                             "rotations, centre distance U[0.2, 0.9](r1 + r2), op U{union, intersect, diff}, seed "
+                             f"{SEED}, weld factor 1e5",
+                 "meshes_per_s": allsum(dist, float(len(pairs))) / allmax(dist, t1 - t0), "s_total": t1 - t0,
+                 "workers": 8, "failed_pairs": int(np.count_nonzero(statuses != 0)),
+                 "timing": "host wall time of one sb_batch_combine call, host inputs"}
     # roofline for the dominant instrumented kernel
     peak, peak_kind = measured_peaks()
     dom = max(kern.items(), key=lambda kv: kv[1][0]) if kern else None
@@ -354,7 +370,7 @@ def gpu_arm(args, rank, world, local, dist):
         "value": value, "ms_per_step": ms32_max, "stats": st32, "stats_fp64": st64, "t64": ms64,
         "codes": sorted(codes), "launches": launches, "clocks": clocks, "roofline": roof,
         "per_kernel": per_kernel, "e2e_s": e2e_s, "h2d": h2d, "d2h": d2h, "res": res,
-        "total_pairs": total_pairs, "sizes": (nva, na, nvb, nb),
+        "total_pairs": total_pairs, "sizes": (nva, na, nvb, nb), "batch": batch,
     }
 
 
@@ -381,6 +397,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-runs", type=int, default=2)
+    ap.add_argument("--batch-pairs", type=int, default=4096, help="pairs of the batched workload (0: skip)")
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -437,6 +454,7 @@ def main():
                 "d2h_bytes_per_step": int(r["d2h"]), "ms_per_step": r["e2e_s"] * 1e3},
         "parity_vs_oracle": parity,
         "clocks": r["clocks"], "gpu_launches": int(r["launches"]),
+        "batch": r["batch"],
     }
     print(json.dumps(line))
 

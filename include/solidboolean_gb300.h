@@ -140,6 +140,23 @@ sb_status sb_retriangulate_faces_noalloc(const double *d_corners, const int *d_s
                                          int *d_tri_count, double *d_points, int *d_point_count, int *d_status,
                                          void *stream);
 
+/* No counterpart in the reference, which combines one pair per call: many independent pairs in one call.
+ * Inputs are host arrays in CSR form: pair i's first mesh has the vertices xyz_a[3*v_off_a[i] ..
+ * 3*v_off_a[i+1]) and the triangles tris_a[3*t_off_a[i] .. 3*t_off_a[i+1]) (vertex indices local to that
+ * mesh); likewise the second mesh; ops[i] (an sb_op) names the result kept for the pair. statuses[i]
+ * receives what sb_combine would return for the pair. Pairs run on `workers` concurrent streams (0: 8), each
+ * with reusable handles. With out non-NULL the results (all result vertices, the op's triangles) are kept
+ * for sb_batch_result_size / sb_batch_result; with out NULL only the statuses are produced. The return value
+ * reports failures of the batch itself (invalid arguments, stream or handle creation). */
+typedef struct sb_batch sb_batch;
+sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_a, const uint32_t *tris_a,
+                           const uint64_t *t_off_a, const double *xyz_b, const uint64_t *v_off_b,
+                           const uint32_t *tris_b, const uint64_t *t_off_b, const int32_t *ops,
+                           const sb_options *opts, int32_t workers, int32_t *statuses, sb_batch **out);
+sb_status sb_batch_result_size(const sb_batch *b, size_t i, size_t *n_vertices, size_t *n_triangles);
+sb_status sb_batch_result(const sb_batch *b, size_t i, double *xyz, uint32_t *tris);
+void sb_batch_destroy(sb_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,14 @@ def lib() -> ctypes.CDLL:
     L.sb_debug_dump.restype = st
     L.sb_debug_dump.argtypes = [vp, ctypes.c_char_p, vp, sz, ctypes.POINTER(sz)]
     L.sb_boolean_destroy.argtypes = [vp]
+    L.sb_batch_combine.restype = st
+    L.sb_batch_combine.argtypes = [sz, vp, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Options), ctypes.c_int32,
+                                   vp, ctypes.POINTER(vp)]
+    L.sb_batch_result_size.restype = st
+    L.sb_batch_result_size.argtypes = [vp, sz, ctypes.POINTER(sz), ctypes.POINTER(sz)]
+    L.sb_batch_result.restype = st
+    L.sb_batch_result.argtypes = [vp, sz, vp, vp]
+    L.sb_batch_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -264,3 +272,52 @@ def run_boolean(va, fa, vb, fb, weld_factor: int = 100000, precision: str = "fil
     for op in ("union", "diff", "intersect"):
         out[op] = sb.fetch(op).astype(np.int64)
     return out
+
+
+OP_CODES = {"union": SB_UNION, "diff": SB_DIFF, "intersect": SB_INTERSECT}
+
+
+def batch_combine(pairs, weld_factor: int = 100000, precision: str = "filtered", order: str = "reference",
+                  workers: int = 8, keep: bool = True):
+    """Many independent booleans in one call (sb_batch_combine). pairs: sequence of (va, fa, vb, fb, op) with
+    op in "union" / "diff" / "intersect". Returns (statuses, results): statuses an int32 array of per-pair
+    sb_combine codes; results (when keep) a list of (result vertices, the op's triangles) per pair, empty
+    arrays for pairs that did not combine."""
+    L = lib()
+    n = len(pairs)
+
+    def csr(items, width, dtype):
+        off = np.zeros(n + 1, dtype=np.uint64)
+        for i, x in enumerate(items):
+            off[i + 1] = off[i] + len(x)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=dtype).reshape(-1, width) for x in items])
+                                    if n else np.zeros((0, width), dtype=dtype))
+        return flat, off
+
+    va, vao = csr([p[0] for p in pairs], 3, np.float64)
+    ta, tao = csr([p[1] for p in pairs], 3, np.uint32)
+    vb, vbo = csr([p[2] for p in pairs], 3, np.float64)
+    tb, tbo = csr([p[3] for p in pairs], 3, np.uint32)
+    ops = np.array([OP_CODES[p[4]] for p in pairs], dtype=np.int32)
+    statuses = np.zeros(n, dtype=np.int32)
+    opts = make_options(weld_factor, precision, order)
+    handle = ctypes.c_void_p()
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    code = L.sb_batch_combine(n, ptr(va), ptr(vao), ptr(ta), ptr(tao), ptr(vb), ptr(vbo), ptr(tb), ptr(tbo),
+                              ptr(ops), ctypes.byref(opts), workers, ptr(statuses),
+                              ctypes.byref(handle) if keep else None)
+    _check(code, "sb_batch_combine")
+    results = None
+    if keep:
+        results = []
+        try:
+            for i in range(n):
+                nv, nt = ctypes.c_size_t(), ctypes.c_size_t()
+                _check(L.sb_batch_result_size(handle, i, ctypes.byref(nv), ctypes.byref(nt)), "sb_batch_result_size")
+                xyz = np.empty((nv.value, 3), dtype=np.float64)
+                tris = np.empty((nt.value, 3), dtype=np.uint32)
+                _check(L.sb_batch_result(handle, i, ptr(xyz), ptr(tris)), "sb_batch_result")
+                results.append((xyz, tris))
+        finally:
+            L.sb_batch_destroy(handle)
+    return statuses, results

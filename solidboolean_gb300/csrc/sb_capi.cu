@@ -8,6 +8,8 @@
 #include <atomic>
 #include <climits>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -71,12 +73,39 @@ sb_status cuda_fail(cudaError_t e, const char *expr, const char *file, int line)
     return SB_ERR_CUDA;
 }
 
+// Device blocks released by handles are kept per device for reuse (handles are created and destroyed per
+// call on the host-buffer path, and cudaMalloc / cudaFree are slow and synchronising). A block goes back to
+// the cache only after the device has finished all queued work, as cudaFree would have waited, so no later
+// owner can overlap an earlier one's kernels. At most kCacheBytes stay cached.
+namespace {
+struct BlockCache {
+    std::mutex mu;
+    std::multimap<std::pair<int, size_t>, void *> free; // (device, bytes) -> block
+    size_t cached = 0;
+};
+BlockCache g_blocks;
+constexpr size_t kCacheBytes = 8ull << 30;
+} // namespace
+
 cudaError_t DevBuf::ensure(size_t need)
 {
     if (need <= bytes && ptr)
         return cudaSuccess;
     release();
-    size_t n = std::max<size_t>(need + need / 4, 1024);
+    const size_t n = std::max<size_t>(need + need / 4, 1024);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(g_blocks.mu);
+        auto it = g_blocks.free.lower_bound({dev, need});
+        if (it != g_blocks.free.end() && it->first.first == dev && it->first.second <= 2 * n) {
+            ptr = it->second;
+            bytes = it->first.second;
+            g_blocks.cached -= bytes;
+            g_blocks.free.erase(it);
+            return cudaSuccess;
+        }
+    }
     cudaError_t e = cudaMalloc(&ptr, n);
     if (e != cudaSuccess) {
         ptr = nullptr;
@@ -89,8 +118,18 @@ cudaError_t DevBuf::ensure(size_t need)
 
 void DevBuf::release()
 {
-    if (ptr)
-        cudaFree(ptr);
+    if (ptr) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceSynchronize(); // queued work may still use the block
+        std::lock_guard<std::mutex> lk(g_blocks.mu);
+        if (g_blocks.cached + bytes <= kCacheBytes) {
+            g_blocks.free.insert({{dev, bytes}, ptr});
+            g_blocks.cached += bytes;
+        } else {
+            cudaFree(ptr);
+        }
+    }
     ptr = nullptr;
     bytes = 0;
 }
@@ -1208,8 +1247,7 @@ void sb_mesh_destroy(sb_mesh *m)
     m->rankTmp.release();
     if (m->rankPending && m->aux)
         cudaStreamSynchronize(m->aux);
-    if (m->rankCheck)
-        cudaFreeHost(m->rankCheck);
+    pinned_slot_release(m->rankCheck);
     if (m->aux)
         cudaStreamDestroy(m->aux);
     if (m->auxFork)
@@ -1421,5 +1459,163 @@ void sb_boolean_destroy(sb_boolean *b)
     }
     delete b;
 }
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------------------------------
+// batched booleans
+// ---------------------------------------------------------------------------------------------------
+struct sb_batch {
+    std::vector<std::vector<double>> xyz;   // per pair: result vertices (empty unless kept and combined)
+    std::vector<std::vector<uint32_t>> tris; // per pair: the triangles of the pair's operation
+};
+
+namespace {
+
+// reuses a mesh handle for new inputs: the buffer grows when needed, everything derived is invalidated
+sb_status mesh_reset(sb_mesh *m, const double *xyz, size_t nv, const uint32_t *tris, size_t nt, cudaStream_t s)
+{
+    if (nv > 0x7FFFFFFFu || nt > 0x2AAAAAAAu) {
+        set_last_error("mesh too large");
+        return SB_ERR_INVALID;
+    }
+    SB_CUDA_CHECK(m->buf.ensure(mesh_bytes((int)nv, (int)nt)));
+    m->d = MeshDev{};
+    m->d.nv = (int)nv;
+    m->d.nt = (int)nt;
+    Carve c;
+    const size_t o_v = c.take<double>(nv * 3), o_t = c.take<uint32_t>(nt * 3);
+    m->d.v = reinterpret_cast<double *>(m->buf.as<char>() + o_v);
+    m->d.t = reinterpret_cast<uint32_t *>(m->buf.as<char>() + o_t);
+    m->prepared = false;
+    m->adjValid = false;
+    m->rankPending = false;
+    if (nv)
+        SB_CUDA_CHECK(cudaMemcpyAsync(m->d.v, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, s));
+    if (nt)
+        SB_CUDA_CHECK(cudaMemcpyAsync(m->d.t, tris, sizeof(uint32_t) * 3 * nt, cudaMemcpyHostToDevice, s));
+    return mesh_validate(m, s);
+}
+
+} // namespace
+
+extern "C" {
+
+sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_a, const uint32_t *tris_a,
+                           const uint64_t *t_off_a, const double *xyz_b, const uint64_t *v_off_b,
+                           const uint32_t *tris_b, const uint64_t *t_off_b, const int32_t *ops,
+                           const sb_options *opts, int32_t workers, int32_t *statuses, sb_batch **out)
+{
+    if (out)
+        *out = nullptr;
+    if (!statuses || (n && (!xyz_a || !v_off_a || !tris_a || !t_off_a || !xyz_b || !v_off_b || !tris_b || !t_off_b ||
+                            !ops)))
+        return SB_ERR_INVALID;
+    return guarded([&]() -> sb_status {
+        sb_options base;
+        sb_default_options(&base);
+        if (opts)
+            base = *opts;
+        std::unique_ptr<sb_batch> keep(out ? new sb_batch : nullptr);
+        if (keep) {
+            keep->xyz.resize(n);
+            keep->tris.resize(n);
+        }
+        const int W = (int)std::max<int64_t>(1, std::min<int64_t>(workers > 0 ? workers : 8, (int64_t)n));
+        std::atomic<size_t> next{0};
+        std::vector<sb_status> setup(W, SB_OK);
+        // one worker: its own stream, a reusable pair of meshes and one boolean handle; pairs taken in turn
+        auto pairs = [&](int w) {
+            cudaStream_t s = nullptr;
+            sb_mesh *ma = nullptr, *mb = nullptr;
+            sb_boolean *x = nullptr;
+            sb_status st = SB_OK;
+            if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+                st = SB_ERR_CUDA;
+            if (st == SB_OK)
+                st = mesh_alloc(0, 0, &ma);
+            if (st == SB_OK)
+                st = mesh_alloc(0, 0, &mb);
+            sb_options o = base;
+            o.stream = s;
+            if (st == SB_OK)
+                st = sb_boolean_create(ma, mb, &o, &x);
+            setup[w] = st;
+            for (size_t i = next++; st == SB_OK && i < n; i = next++) {
+                const int op = ops[i];
+                sb_status r = (op < SB_UNION || op > SB_INTERSECT) ? SB_ERR_INVALID : SB_OK;
+                if (r == SB_OK)
+                    r = mesh_reset(ma, xyz_a + 3 * v_off_a[i], v_off_a[i + 1] - v_off_a[i], tris_a + 3 * t_off_a[i],
+                                   t_off_a[i + 1] - t_off_a[i], s);
+                if (r == SB_OK)
+                    r = mesh_reset(mb, xyz_b + 3 * v_off_b[i], v_off_b[i + 1] - v_off_b[i], tris_b + 3 * t_off_b[i],
+                                   t_off_b[i + 1] - t_off_b[i], s);
+                if (r == SB_OK)
+                    r = sb_combine(x, nullptr);
+                statuses[i] = r;
+                if (keep && r == SB_OK) {
+                    size_t nv = 0, nt = 0;
+                    sb_status q = sb_result_vertices(x, nullptr, 0, &nv);
+                    if (q == SB_OK)
+                        q = sb_fetch(x, (sb_op)op, nullptr, 0, &nt);
+                    if (q == SB_OK) {
+                        keep->xyz[i].resize(3 * nv);
+                        keep->tris[i].resize(3 * nt);
+                        q = sb_result_vertices(x, keep->xyz[i].data(), nv, &nv);
+                    }
+                    if (q == SB_OK)
+                        q = sb_fetch(x, (sb_op)op, keep->tris[i].data(), nt, &nt);
+                    if (q != SB_OK)
+                        statuses[i] = q;
+                }
+            }
+            if (x)
+                sb_boolean_destroy(x);
+            sb_mesh_destroy(ma);
+            sb_mesh_destroy(mb);
+            if (s)
+                cudaStreamDestroy(s);
+        };
+        auto work = [&](int w) {
+            try {
+                pairs(w);
+            } catch (...) {
+                setup[w] = SB_ERR_INVALID;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < W; ++w)
+            pool.emplace_back(work, w);
+        work(0);
+        for (auto &t : pool)
+            t.join();
+        for (int w = 0; w < W; ++w)
+            if (setup[w] != SB_OK)
+                return setup[w];
+        if (out)
+            *out = keep.release();
+        return SB_OK;
+    });
+}
+
+sb_status sb_batch_result_size(const sb_batch *b, size_t i, size_t *n_vertices, size_t *n_triangles)
+{
+    if (!b || i >= b->xyz.size() || !n_vertices || !n_triangles)
+        return SB_ERR_INVALID;
+    *n_vertices = b->xyz[i].size() / 3;
+    *n_triangles = b->tris[i].size() / 3;
+    return SB_OK;
+}
+
+sb_status sb_batch_result(const sb_batch *b, size_t i, double *xyz, uint32_t *tris)
+{
+    if (!b || i >= b->xyz.size() || (!xyz && !b->xyz[i].empty()) || (!tris && !b->tris[i].empty()))
+        return SB_ERR_INVALID;
+    std::copy(b->xyz[i].begin(), b->xyz[i].end(), xyz);
+    std::copy(b->tris[i].begin(), b->tris[i].end(), tris);
+    return SB_OK;
+}
+
+void sb_batch_destroy(sb_batch *b) { delete b; }
 
 } // extern "C"

@@ -30,7 +30,9 @@
 // long runs for the reductions; one radix sort then lists each remaining node's members in order, and one
 // block per such node finishes its subtree in shared memory and writes the final positions.
 #include <algorithm>
+#include <condition_variable>
 #include <mutex>
+#include <vector>
 
 #include <cub/cub.cuh>
 
@@ -1250,7 +1252,40 @@ static int bit_length(int x)
 // Blocks of the cooperative large-node kernel: half of what can be resident at once (the two meshes of a
 // boolean are prepared concurrently, so two such grids must fit together), no more than the members need.
 // Cached per device.
-static int top_grid(int nt)
+// Cooperative blocks of k_rr_top in flight per device. Cooperative grids launched from several streams at
+// once (two meshes of a boolean, batched booleans) must fit on the device together, or resident blocks of
+// one could wait at a grid barrier for blocks that cannot be scheduled; a launch therefore waits until its
+// blocks fit in the budget, and a host callback on its stream returns them when the kernel has finished.
+struct CoopBudget {
+    std::mutex mu;
+    std::condition_variable cv;
+    int capacity[256] = {0}, inFlight[256] = {0};
+};
+static CoopBudget g_coop;
+
+struct CoopRelease {
+    int dev, blocks;
+};
+
+static void CUDART_CB coop_release(void *p)
+{
+    CoopRelease *r = static_cast<CoopRelease *>(p);
+    {
+        std::lock_guard<std::mutex> lk(g_coop.mu);
+        g_coop.inFlight[r->dev] -= r->blocks;
+    }
+    g_coop.cv.notify_all();
+    delete r;
+}
+
+static void coop_acquire(int dev, int blocks)
+{
+    std::unique_lock<std::mutex> lk(g_coop.mu);
+    g_coop.cv.wait(lk, [&] { return g_coop.inFlight[dev] + blocks <= g_coop.capacity[dev]; });
+    g_coop.inFlight[dev] += blocks;
+}
+
+static int top_grid(int nt, int *devOut)
 {
     static int perSm[256], sms[256];
     static std::mutex mu;
@@ -1269,8 +1304,11 @@ static int top_grid(int nt)
                 perSm[dev] = 0;
                 return -1;
             }
+            std::lock_guard<std::mutex> lk2(g_coop.mu);
+            g_coop.capacity[dev] = perSm[dev] * sms[dev];
         }
     }
+    *devOut = dev;
     const int need = (nt + kElemThreads * 4 - 1) / (kElemThreads * 4); // at least 4 members per thread
     return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 2)));
 }
@@ -1296,6 +1334,39 @@ static sb_status rank_status(const int *chk)
         return SB_ERR_CAPACITY;
     }
     return SB_OK;
+}
+
+// Pinned 16-int slots for the leaf-order status of each mesh, carved from one block allocated once per
+// process: pinned allocations are slow and synchronising, and meshes come and go.
+static std::mutex g_pinMu;
+static int *g_pinBlock = nullptr;
+static std::vector<int *> g_pinFree;
+constexpr int kPinSlots = 4096;
+
+int *pinned_slot_acquire()
+{
+    std::lock_guard<std::mutex> lk(g_pinMu);
+    if (!g_pinBlock) {
+        if (cudaMallocHost((void **)&g_pinBlock, sizeof(int) * 16 * kPinSlots) != cudaSuccess) {
+            g_pinBlock = nullptr;
+            return nullptr;
+        }
+        for (int i = kPinSlots - 1; i >= 0; --i)
+            g_pinFree.push_back(g_pinBlock + 16 * i);
+    }
+    if (g_pinFree.empty())
+        return nullptr;
+    int *p = g_pinFree.back();
+    g_pinFree.pop_back();
+    return p;
+}
+
+void pinned_slot_release(int *p)
+{
+    if (!p)
+        return;
+    std::lock_guard<std::mutex> lk(g_pinMu);
+    g_pinFree.push_back(p);
 }
 
 sb_status reference_rank_result(sb_mesh *m)
@@ -1353,14 +1424,23 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, np, nt, scg, counters, terms);
     // the large-node phase: one cooperative launch, every block resident
     if (nt > kSub) {
-        const int topBlocks = top_grid(nt);
+        int dev = 0;
+        const int topBlocks = top_grid(nt, &dev);
         if (topBlocks <= 0)
             return SB_ERR_CUDA;
+        coop_acquire(dev, topBlocks);
         void *args[] = {(void *)&nt, (void *)&rec, (void *)&soa, (void *)&state, (void *)&np, (void *)&nodes, (void *)&counters,
                         (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar};
         count_launch();
         KTime kt("k_rr_top", s);
-        SB_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)k_rr_top, dim3(topBlocks), dim3(kElemThreads), args, 0, s));
+        const cudaError_t le =
+            cudaLaunchCooperativeKernel((const void *)k_rr_top, dim3(topBlocks), dim3(kElemThreads), args, 0, s);
+        const cudaError_t ce = le == cudaSuccess ? cudaLaunchHostFunc(s, coop_release, new CoopRelease{dev, topBlocks})
+                                                 : le;
+        if (ce != cudaSuccess) {
+            coop_release(new CoopRelease{dev, topBlocks}); // no callback will return them
+            SB_CUDA_CHECK(ce);
+        }
     }
     SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
@@ -1374,8 +1454,13 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     }
     // counters and barrier record to pinned host memory; read now, or by reference_rank_result once the
     // caller has synchronised past this stream
-    if (!m->rankCheck)
-        SB_CUDA_CHECK(cudaMallocHost((void **)&m->rankCheck, 16 * sizeof(int)));
+    if (!m->rankCheck) {
+        m->rankCheck = pinned_slot_acquire();
+        if (!m->rankCheck) {
+            set_last_error("no pinned host memory for the leaf-order status");
+            return SB_ERR_CUDA;
+        }
+    }
     SB_CUDA_CHECK(cudaMemcpyAsync(m->rankCheck, counters, kCtCount * sizeof(int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaMemcpyAsync(m->rankCheck + kCtCount, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaGetLastError());
