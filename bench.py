@@ -352,6 +352,51 @@ def gpu_arm(args, rank, world, local, dist):
                  "meshes_per_s": allsum(dist, float(len(pairs))) / allmax(dist, t1 - t0), "s_total": t1 - t0,
                  "workers": 8, "failed_pairs": int(np.count_nonzero(statuses != 0)),
                  "timing": "host wall time of one sb_batch_combine call, host inputs"}
+
+    # differentiable workload: intersection of two level-5 icospheres (B offset by seeded N(0, 0.01^2)),
+    # forward (combine) and adjoint (sb_adjoint with a unit gradient on every result vertex), CUDA events
+    adj = None
+    if args.adjoint:
+        ua, ufa, ub, ufb, uoff = mg.diff_volume(SEED, 5)
+        ub = ub + uoff
+        dv = [torch.from_numpy(x).to(dev) for x in (ua, ub)]
+        dt = [torch.from_numpy(x.astype(np.int32)).to(dev) for x in (ufa, ufb)]
+        o5 = sbg.make_options(WELD, "filtered", "reference", stream.cuda_stream)
+        h5 = [ctypes.c_void_p() for _ in range(3)]
+        sbg._check(L.sb_mesh_create_device(dv[0].data_ptr(), len(ua), dt[0].data_ptr(), len(ufa), ctypes.byref(o5),
+                                           ctypes.byref(h5[0])), "A5")
+        sbg._check(L.sb_mesh_create_device(dv[1].data_ptr(), len(ub), dt[1].data_ptr(), len(ufb), ctypes.byref(o5),
+                                           ctypes.byref(h5[1])), "B5")
+        sbg._check(L.sb_boolean_create(h5[0], h5[1], ctypes.byref(o5), ctypes.byref(h5[2])), "X5")
+        st5 = sbg.Stats()
+        tf, tb = [], []
+        ga, gb = torch.zeros_like(dv[0]), torch.zeros_like(dv[1])
+        for it in range(args.warmup + args.steps):
+            sbg._check(L.sb_mesh_update_vertices_device(h5[0], dv[0].data_ptr(), ctypes.byref(o5)), "u5")
+            sbg._check(L.sb_mesh_update_vertices_device(h5[1], dv[1].data_ptr(), ctypes.byref(o5)), "u5")
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            sbg._check(L.sb_combine(h5[2], ctypes.byref(st5)), "combine5")
+            e1.record(stream)
+            gv = torch.ones((int(st5.result_vertices), 3), dtype=torch.float64, device=dev)
+            ga.zero_()
+            gb.zero_()
+            torch.cuda.synchronize()
+            e1b = torch.cuda.Event(enable_timing=True)
+            e1b.record(stream)
+            sbg._check(L.sb_adjoint(h5[2], gv.data_ptr(), ga.data_ptr(), gb.data_ptr(), stream.cuda_stream), "adj")
+            e2.record(stream)
+            e2.synchronize()
+            if it >= args.warmup:
+                tf.append(e0.elapsed_time(e1))
+                tb.append(e1b.elapsed_time(e2))
+        L.sb_boolean_destroy(h5[2])
+        L.sb_mesh_destroy(h5[0])
+        L.sb_mesh_destroy(h5[1])
+        adj = {"workload": "intersection of two icospheres L5 (20,480 t each), r 1 and 0.85, offset (0.35, 0, 0), "
+                           "B offsets N(0, 0.01^2) seed 1234, weld factor 1e8",
+               "forward_ms": statistics.mean(tf), "adjoint_ms": statistics.mean(tb),
+               "appended_vertices": int(st5.new_points)}
     # roofline for the dominant instrumented kernel
     peak, peak_kind = measured_peaks()
     dom = max(kern.items(), key=lambda kv: kv[1][0]) if kern else None
@@ -370,7 +415,7 @@ def gpu_arm(args, rank, world, local, dist):
         "value": value, "ms_per_step": ms32_max, "stats": st32, "stats_fp64": st64, "t64": ms64,
         "codes": sorted(codes), "launches": launches, "clocks": clocks, "roofline": roof,
         "per_kernel": per_kernel, "e2e_s": e2e_s, "h2d": h2d, "d2h": d2h, "res": res,
-        "total_pairs": total_pairs, "sizes": (nva, na, nvb, nb), "batch": batch,
+        "total_pairs": total_pairs, "sizes": (nva, na, nvb, nb), "batch": batch, "adjoint": adj,
     }
 
 
@@ -398,6 +443,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-runs", type=int, default=2)
     ap.add_argument("--batch-pairs", type=int, default=4096, help="pairs of the batched workload (0: skip)")
+    ap.add_argument("--adjoint", type=int, default=1, help="time forward + adjoint on the differentiable workload")
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -454,7 +500,7 @@ def main():
                 "d2h_bytes_per_step": int(r["d2h"]), "ms_per_step": r["e2e_s"] * 1e3},
         "parity_vs_oracle": parity,
         "clocks": r["clocks"], "gpu_launches": int(r["launches"]),
-        "batch": r["batch"],
+        "batch": r["batch"], "adjoint": r["adjoint"],
     }
     print(json.dumps(line))
 

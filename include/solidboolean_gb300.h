@@ -148,6 +148,17 @@ sb_status sb_retriangulate_faces_noalloc(const double *d_corners, const int *d_s
  * with reusable handles. With out non-NULL the results (all result vertices, the op's triangles) are kept
  * for sb_batch_result_size / sb_batch_result; with out NULL only the statuses are produced. The return value
  * reports failures of the batch itself (invalid arguments, stream or handle creation). */
+/* No counterpart in the reference. Adjoint of the last sb_combine with its combinatorics held fixed: given
+ * d_grad_result, the gradient of a loss with respect to every result vertex ([n*3] doubles on the device, in
+ * sb_result_vertices order), adds the loss's gradient with respect to the input vertices to d_grad_first
+ * ([nv_first*3]) and d_grad_second ([nv_second*3]) on the device (the caller zeroes them). An input vertex
+ * passes its own gradient through; an appended vertex passes its gradient through the construction of the
+ * intersection point that represents it (segment end p - a (p - r), a a ratio of dot products with a
+ * triangle normal) to the six vertices of that triangle pair. Requires a combine that returned SB_OK;
+ * runs on `stream` and does not synchronise. */
+sb_status sb_adjoint(sb_boolean *b, const double *d_grad_result, double *d_grad_first, double *d_grad_second,
+                     void *stream);
+
 typedef struct sb_batch sb_batch;
 sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_a, const uint32_t *tris_a,
                            const uint64_t *t_off_a, const double *xyz_b, const uint64_t *v_off_b,

@@ -105,6 +105,8 @@ def lib() -> ctypes.CDLL:
     L.sb_batch_result.restype = st
     L.sb_batch_result.argtypes = [vp, sz, vp, vp]
     L.sb_batch_destroy.argtypes = [vp]
+    L.sb_adjoint.restype = st
+    L.sb_adjoint.argtypes = [vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -65,13 +65,14 @@ __global__ void k_weld_first(int nFaces, const int *__restrict__ ptOff, const in
 
 __global__ void k_weld_number(int nSeq, const int *__restrict__ isFirst, const int *__restrict__ firstRank,
                               const int *__restrict__ pointSlot, int *slotRank, const d3 *__restrict__ pts,
-                              double *newV, int vbase)
+                              double *newV, int vbase, const int *__restrict__ ptSrc, int *newSrc)
 {
     int seq = blockIdx.x * blockDim.x + threadIdx.x;
     if (seq >= nSeq || !isFirst[seq])
         return;
     int r = firstRank[seq];
     slotRank[pointSlot[seq]] = r;
+    newSrc[r] = ptSrc[seq];
     d3 p = pts[seq];
     double *o = newV + 3 * (size_t)(vbase + r);
     o[0] = p.x;
@@ -792,7 +793,7 @@ void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s)
     {
         KTime kt("k_weld_number", s);
         SB_COUNT(k_weld_number)<<<nb(nSeq, 256), 256, 0, s>>>(nSeq, g.isFirst, g.firstRank, g.pointSlot, g.slotRank, g.cutPts,
-                                                g.newV, g.newBase);
+                                                g.newV, g.newBase, g.ptSrc, g.newSrc);
     }
 }
 

@@ -30,6 +30,8 @@ struct AsmArgs {
     uint32_t weldMask;
     int *pointSlot, *isFirst, *firstRank, *slotRank;
     int newBase; // = A.nv + B.nv
+    const int *ptSrc; // per cut point: 2 x (intersecting pair) + segment end (see FaceArgs::ptSrc)
+    int *newSrc;      // per appended vertex: the source of the point that represents its weld class
     int nNew;    // unique cut points
     double *newV;
     // arrangement

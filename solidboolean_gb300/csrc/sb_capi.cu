@@ -200,8 +200,8 @@ __global__ void k_fill_u64(size_t n, uint64_t *a, uint64_t v)
 // key) and inside the second mesh's face (by the first triangle's order key)
 __global__ void k_pair_keys(int K, const int *__restrict__ sel, const uint64_t *__restrict__ cand, int nB,
                             const int *__restrict__ rankA, const int *__restrict__ rankB,
-                            const double *__restrict__ seg, uint64_t *keyA, uint64_t *keyB, int *val, double *segK,
-                            uint32_t *pairAB)
+                            const double *__restrict__ seg, const uint32_t *__restrict__ perm, uint64_t *keyA,
+                            uint64_t *keyB, int *val, double *segK, uint32_t *pairAB, uint32_t *pairPerm)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= K)
@@ -219,6 +219,7 @@ __global__ void k_pair_keys(int K, const int *__restrict__ sel, const uint64_t *
         segK[6 * (size_t)j + k] = seg[6 * (size_t)idx + k];
     pairAB[2 * (size_t)j] = a;
     pairAB[2 * (size_t)j + 1] = b;
+    pairPerm[j] = perm[idx];
 }
 
 __global__ void k_hi32(int n, const uint64_t *__restrict__ k, int *out)
@@ -319,6 +320,101 @@ __global__ void __launch_bounds__(kGroupThreads)
         ct[r] = sm.starts[r + 1] - sm.starts[r];
     if (threadIdx.x == 0)
         runCount[side] = (unsigned int)total;
+}
+
+// ---- adjoint of the combine, its combinatorics held fixed --------------------------------------------
+// An appended vertex is the representative of its weld class, a segment end built by CONSTRUCT_INTERSECTION
+// (tri_tri_intersect.c:285-356) as x = b - a (b - o), a = ((b - r).N) / ((b - o).N), with b, r, o three of
+// the pair's six vertices and N the normal cross(P1 - P0, P2 - P0) of the first triangle or
+// cross(P3 - P5, P4 - P5) of the second. With u = b - r, w = b - o, D = w.N and c = -(g.w) / D for the
+// upstream gradient g:  dL/db = (1 - a)(g + cN), dL/dr = -cN, dL/do = a (g + cN), dL/dN = c (u - a w);
+// dL/dN reaches the triangle's vertices through the cross product. Input vertices keep their gradient.
+__device__ __forceinline__ void atomic_add3(double *p, d3 v)
+{
+    atomicAdd(p, v.x);
+    atomicAdd(p + 1, v.y);
+    atomicAdd(p + 2, v.z);
+}
+
+__global__ void k_adjoint(size_t nv, int nvA, int nvB, const double *__restrict__ grad, const int *__restrict__ newSrc,
+                          const uint32_t *__restrict__ pairAB, const uint32_t *__restrict__ pairPerm, MeshDev A,
+                          MeshDev B, double *gradA, double *gradB)
+{
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= nv)
+        return;
+    const d3 g = mk(grad[3 * i], grad[3 * i + 1], grad[3 * i + 2]);
+    if (i < (size_t)nvA) {
+        atomic_add3(gradA + 3 * i, g);
+        return;
+    }
+    if (i < (size_t)nvA + nvB) {
+        atomic_add3(gradB + 3 * (i - nvA), g);
+        return;
+    }
+    const int src = newSrc[i - nvA - nvB];
+    const int j = src >> 1, end = src & 1;
+    const uint32_t code = pairPerm[j];
+    int slot[6];
+    for (int k = 0; k < 6; ++k)
+        slot[k] = (int)((code >> (3 * k)) & 7u);
+    const int which = (int)((code >> 18) & 3u);
+    // vertex of each physical slot: 0..2 the first triangle, 3..5 the second
+    const uint32_t ta = pairAB[2 * (size_t)j], tb = pairAB[2 * (size_t)j + 1];
+    int vid[6];
+    d3 P[6];
+    for (int k = 0; k < 3; ++k) {
+        vid[k] = (int)A.t[3 * (size_t)ta + k];
+        vid[3 + k] = (int)B.t[3 * (size_t)tb + k];
+        P[k] = mk(A.v[3 * (size_t)vid[k]], A.v[3 * (size_t)vid[k] + 1], A.v[3 * (size_t)vid[k] + 2]);
+        P[3 + k] = mk(B.v[3 * (size_t)vid[3 + k]], B.v[3 * (size_t)vid[3 + k] + 1], B.v[3 * (size_t)vid[3 + k] + 2]);
+    }
+    const int p1 = slot[0], q1 = slot[1], r1 = slot[2], p2 = slot[3], q2 = slot[4], r2 = slot[5];
+    int sb, sr, so, tri; // base, ref, other, normal of triangle 0 (first) or 1 (second)
+    if (end == 0) {
+        const bool on1 = which == 0 || which == 2;
+        sb = on1 ? p1 : p2;
+        sr = on1 ? p2 : p1;
+        so = on1 ? r1 : q2;
+        tri = on1 ? 1 : 0;
+    } else {
+        const bool on2 = which <= 1;
+        sb = on2 ? p2 : p1;
+        sr = on2 ? p1 : p2;
+        so = on2 ? r2 : q1;
+        tri = on2 ? 0 : 1;
+    }
+    const d3 e1 = tri == 0 ? P[1] - P[0] : P[3] - P[5];
+    const d3 e2 = tri == 0 ? P[2] - P[0] : P[4] - P[5];
+    const d3 N = cross(e1, e2);
+    const d3 u = P[sb] - P[sr], w = P[sb] - P[so];
+    const double D = dot(w, N);
+    if (D == 0.0)
+        return; // a degenerate construction the forward pass could not have produced finitely
+    const double al = dot(u, N) / D;
+    const double c = -dot(g, w) / D;
+    const d3 gc = g + scale(c, N);
+    d3 gP[6];
+    for (int k = 0; k < 6; ++k)
+        gP[k] = mk(0, 0, 0);
+    gP[sb] = gP[sb] + scale(1.0 - al, gc);
+    gP[sr] = gP[sr] - scale(c, N);
+    gP[so] = gP[so] + scale(al, gc);
+    const d3 gN = scale(c, u - scale(al, w));
+    const d3 ge1 = cross(e2, gN), ge2 = cross(gN, e1); // N = e1 x e2
+    if (tri == 0) {
+        gP[1] = gP[1] + ge1;
+        gP[2] = gP[2] + ge2;
+        gP[0] = gP[0] - (ge1 + ge2);
+    } else {
+        gP[3] = gP[3] + ge1;
+        gP[4] = gP[4] + ge2;
+        gP[5] = gP[5] - (ge1 + ge2);
+    }
+    for (int k = 0; k < 3; ++k) {
+        atomic_add3(gradA + 3 * (size_t)vid[k], gP[k]);
+        atomic_add3(gradB + 3 * (size_t)vid[3 + k], gP[3 + k]);
+    }
 }
 
 __global__ void k_face_table(int FA, int FB, const int *__restrict__ uniqA, const int *__restrict__ cntA,
@@ -432,6 +528,11 @@ struct sb_boolean {
     int C = 0, K = 0;
     uint32_t *d_pairAB = nullptr;
     double *d_segK = nullptr;
+    // for the adjoint: each intersecting pair's construction record, and the source (2 x pair + segment end)
+    // of every appended vertex
+    uint32_t *d_pairPerm = nullptr;
+    int *d_newSrc = nullptr;
+    int newBase = 0;
     double *d_newV = nullptr;
     size_t nNewV = 0;
     uint32_t *d_newT = nullptr;
@@ -532,6 +633,7 @@ sb_status combine_impl(sb_boolean *b)
         size_t o_hit = c.take<uint8_t>(b->candCap);
         size_t o_seg = c.take<double>((size_t)b->candCap * 6);
         size_t o_sel = c.take<int>(b->candCap);
+        c.take<uint32_t>(b->candCap); // per-candidate construction record
         SB_CUDA_CHECK(b->cand.ensure(c.off));
         (void)o_hit;
         (void)o_seg;
@@ -558,11 +660,13 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_hit = cc.take<uint8_t>(b->candCap);
     size_t o_seg = cc.take<double>((size_t)b->candCap * 6);
     size_t o_sel = cc.take<int>(b->candCap);
+    size_t o_perm = cc.take<uint32_t>(b->candCap);
     uint64_t *candRaw = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw);
     uint64_t *candSorted = reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_srt); // unused, see below
     uint8_t *hit = reinterpret_cast<uint8_t *>(b->cand.as<char>() + o_hit);
     double *seg = reinterpret_cast<double *>(b->cand.as<char>() + o_seg);
     int *sel = reinterpret_cast<int *>(b->cand.as<char>() + o_sel);
+    uint32_t *perm = reinterpret_cast<uint32_t *>(b->cand.as<char>() + o_perm);
     // Candidates stay in emission order: every later ordering is by unique keys (face, the other triangle's
     // leaf position), so the result does not depend on it.
     (void)candSorted;
@@ -573,7 +677,7 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaEventRecord(b->ev[1], s));
 
     // ---------------- narrow phase ----------------
-    launch_narrow(fp64, A, B, candSorted, (int)C, hit, seg, d_stats, s);
+    launch_narrow(fp64, A, B, candSorted, (int)C, hit, seg, perm, d_stats, s);
     SB_CUDA_CHECK(cudaGetLastError());
     if (C > 0)
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
@@ -596,6 +700,7 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_keyAs = ci.take<uint64_t>(K + 1), o_keyBs = ci.take<uint64_t>(K + 1);
     size_t o_val = ci.take<int>(K + 1), o_pidx = ci.take<int>(2 * (size_t)K + 2);
     size_t o_segK = ci.take<double>(6 * (size_t)K + 6), o_ab = ci.take<uint32_t>(2 * (size_t)K + 2);
+    size_t o_pp = ci.take<uint32_t>((size_t)K + 1);
     size_t o_hiA = ci.take<int>(K + 1), o_hiB = ci.take<int>(K + 1);
     size_t o_uqA = ci.take<int>(K + 1), o_uqB = ci.take<int>(K + 1);
     size_t o_ctA = ci.take<int>(K + 1), o_ctB = ci.take<int>(K + 1);
@@ -609,6 +714,8 @@ sb_status combine_impl(sb_boolean *b)
     int *hiA = (int *)(ib + o_hiA), *hiB = (int *)(ib + o_hiB);
     int *uqA = (int *)(ib + o_uqA), *uqB = (int *)(ib + o_uqB), *ctA = (int *)(ib + o_ctA), *ctB = (int *)(ib + o_ctB);
     b->d_pairAB = pairAB;
+    uint32_t *pairPerm = (uint32_t *)(ib + o_pp);
+    b->d_pairPerm = pairPerm;
     b->d_segK = segK;
     // the leaf orders may still be building on the meshes' second streams (they overlap the broad and
     // narrow phases); from here on the stream waits for them
@@ -627,7 +734,8 @@ sb_status combine_impl(sb_boolean *b)
     int FA = 0, FB = 0;
     if (K > 0) {
         SB_COUNT(k_pair_keys)<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
-                                                   useRank ? B.rank : nullptr, seg, keyA, keyB, val, segK, pairAB);
+                                                   useRank ? B.rank : nullptr, seg, perm, keyA, keyB, val, segK,
+                                                   pairAB, pairPerm);
         if (K <= (unsigned int)kGroupMax) {
             const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
             const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
@@ -722,11 +830,13 @@ sb_status combine_impl(sb_boolean *b)
     }
     Carve cu;
     size_t o_cp = cu.take<d3>(totals[1] + 1), o_ck = cu.take<Key>(totals[1] + 1);
+    size_t o_psrc = cu.take<int>(totals[1] + 1);
     size_t o_ft = cu.take<int>(3 * totals[2] + 3), o_fe = cu.take<int>(2 * totals[3] + 2);
     SB_CUDA_CHECK(b->cut.ensure(cu.off));
     SB_CUDA_CHECK(b->scratch.ensure((size_t)totals[0] + 256));
     d3 *cutPts = (d3 *)(b->cut.as<char>() + o_cp);
     Key *cutKeys = (Key *)(b->cut.as<char>() + o_ck);
+    int *ptSrc = (int *)(b->cut.as<char>() + o_psrc);
     int *faceTris = (int *)(b->cut.as<char>() + o_ft);
     int *faceEdges = (int *)(b->cut.as<char>() + o_fe);
     if (nFaces > 0) {
@@ -753,6 +863,7 @@ sb_status combine_impl(sb_boolean *b)
         fa.faceNpts = faceNpts;
         fa.faceNtris = faceNtris;
         fa.faceNedges = faceNedges;
+        fa.ptSrc = ptSrc;
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }
@@ -790,6 +901,7 @@ sb_status combine_impl(sb_boolean *b)
     Carve cw;
     size_t o_wo = cw.take<int>(weldCap), o_wm = cw.take<int>(weldCap), o_ps = cw.take<int>(nSeq + 1);
     size_t o_if = cw.take<int>(nSeq + 1), o_fr = cw.take<int>(nSeq + 1), o_sr = cw.take<int>(weldCap);
+    size_t o_nsrc = cw.take<int>(nSeq + 1);
     SB_CUDA_CHECK(b->weld.ensure(cw.off));
     char *wb = b->weld.as<char>();
     g.weldOwner = (int *)(wb + o_wo);
@@ -799,6 +911,10 @@ sb_status combine_impl(sb_boolean *b)
     g.isFirst = (int *)(wb + o_if);
     g.firstRank = (int *)(wb + o_fr);
     g.slotRank = (int *)(wb + o_sr);
+    g.ptSrc = ptSrc;
+    g.newSrc = (int *)(wb + o_nsrc);
+    b->d_newSrc = g.newSrc;
+    b->newBase = A.nv + B.nv;
     SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldOwner, -1);
     SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldMin, INT_MAX);
     SB_CUDA_CHECK(cudaMemsetAsync(g.isFirst, 0, sizeof(int) * (nSeq + 1), s));
@@ -1617,5 +1733,26 @@ sb_status sb_batch_result(const sb_batch *b, size_t i, double *xyz, uint32_t *tr
 }
 
 void sb_batch_destroy(sb_batch *b) { delete b; }
+
+sb_status sb_adjoint(sb_boolean *b, const double *d_grad_result, double *d_grad_first, double *d_grad_second,
+                     void *stream)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (b->status != SB_OK || !d_grad_result || !d_grad_first || !d_grad_second)
+        return SB_ERR_INVALID;
+    return guarded([&]() -> sb_status {
+        const MeshDev &A = b->first->d, &B = b->second->d;
+        if (b->nNewV > 0) {
+            const int bs = 256;
+            SB_COUNT(k_adjoint)<<<(unsigned)((b->nNewV + bs - 1) / bs), bs, 0, (cudaStream_t)stream>>>(
+                b->nNewV, A.nv, B.nv, d_grad_result, b->d_newSrc, b->d_pairAB, b->d_pairPerm, A, B, d_grad_first,
+                d_grad_second);
+        }
+        SB_CUDA_CHECK(cudaGetLastError());
+        return SB_OK;
+    });
+}
 
 } // extern "C"

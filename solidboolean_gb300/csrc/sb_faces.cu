@@ -183,7 +183,8 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
     // ---- 1. local weld: first inserted value of a key wins --------------------------------------------
     int m = 0;
     for (int k = 0; k < np; ++k) {
-        const double *sg = a.segs + 6 * (size_t)a.pairIdx[job.pairBegin + k];
+        const int pair = a.pairIdx[job.pairBegin + k];
+        const double *sg = a.segs + 6 * (size_t)pair;
         int ids[2];
         for (int e = 0; e < 2; ++e) {
             d3 p = mk(sg[3 * e], sg[3 * e + 1], sg[3 * e + 2]);
@@ -198,6 +199,8 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
                 id = m++;
                 outPts[id] = p;
                 outKeys[id] = key;
+                if (a.ptSrc)
+                    a.ptSrc[a.ptOff[f] + id] = 2 * pair + e;
             }
             ids[e] = 3 + id;
         }

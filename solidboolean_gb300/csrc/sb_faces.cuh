@@ -24,6 +24,7 @@ struct FaceArgs {
     int *faceTris;                             // local ids, 3 per triangle
     int *faceEdges;                            // local ids, 2 per edge
     int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
+    int *ptSrc = nullptr; // optional, per face point: 2 x (intersecting pair) + segment end it came from
 };
 
 size_t face_scratch_bytes_host(int np);

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128) k_broad(MeshDev A, MeshDev B, uint64_t *o
 template <bool FP64>
 __global__ void __launch_bounds__(128) k_narrow(MeshDev A, MeshDev B, const uint64_t *__restrict__ cand, int n,
                                                 uint8_t *__restrict__ hit, double *__restrict__ seg,
-                                                unsigned long long *stats)
+                                                uint32_t *__restrict__ perm, unsigned long long *stats)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned int tests = 0, fallbacks = 0;
@@ -156,9 +156,11 @@ __global__ void __launch_bounds__(128) k_narrow(MeshDev A, MeshDev B, const uint
         double s[6];
         int r = tt.run(s);
         hit[i] = r == 1 ? 1 : 0;
-        if (r == 1)
+        if (r == 1) {
             for (int k = 0; k < 6; ++k)
                 seg[6 * (size_t)i + k] = s[k];
+            perm[i] = tt.permCode;
+        }
         tests = tt.tests;
         fallbacks = tt.fallbacks;
     }
@@ -188,7 +190,7 @@ void launch_broad(bool fp64, const MeshDev &A, const MeshDev &B, uint64_t *out, 
 }
 
 void launch_narrow(bool fp64, const MeshDev &A, const MeshDev &B, const uint64_t *cand, int n, uint8_t *hit,
-                   double *seg, unsigned long long *stats, cudaStream_t s)
+                   double *seg, uint32_t *perm, unsigned long long *stats, cudaStream_t s)
 {
     if (n <= 0)
         return;
@@ -196,9 +198,9 @@ void launch_narrow(bool fp64, const MeshDev &A, const MeshDev &B, const uint64_t
     KTime kt("k_narrow", s);
     count_launch();
     if (fp64)
-        k_narrow<true><<<g, bs, 0, s>>>(A, B, cand, n, hit, seg, stats);
+        k_narrow<true><<<g, bs, 0, s>>>(A, B, cand, n, hit, seg, perm, stats);
     else
-        k_narrow<false><<<g, bs, 0, s>>>(A, B, cand, n, hit, seg, stats);
+        k_narrow<false><<<g, bs, 0, s>>>(A, B, cand, n, hit, seg, perm, stats);
 }
 
 } // namespace sbg

@@ -80,6 +80,9 @@ template <bool FP64> struct TriTri {
     float4 F[6];
     bool have64 = false;
     unsigned int tests = 0, fallbacks = 0;
+    // how the segment was built (kept for the adjoint): the six slots in construction order, 3 bits each,
+    // and the case `which` in bits 18-19
+    uint32_t permCode = 0;
     const MeshDev *pA = nullptr, *pB = nullptr;
     int ia[3], ib[3];
 
@@ -208,6 +211,8 @@ template <bool FP64> struct TriTri {
             which = orient(p2, p1, r1, p1, q2, p1) >= 0 ? 2 : 3;
         }
         load64();
+        permCode = (uint32_t)v[0] | (uint32_t)v[1] << 3 | (uint32_t)v[2] << 6 | (uint32_t)v[3] << 9 |
+                   (uint32_t)v[4] << 12 | (uint32_t)v[5] << 15 | (uint32_t)which << 18;
         const d3 N1 = cross(ps(1) - ps(0), ps(2) - ps(0));
         const d3 N2 = cross(ps(3) - ps(5), ps(4) - ps(5));
         // first end point: which 0, 2 -> along(p1, p2, r1, N2); 1, 3 -> along(p2, p1, q2, N1)
@@ -366,6 +371,6 @@ template <bool FP64> struct TriTri {
 void launch_broad(bool fp64, const MeshDev &A, const MeshDev &B, uint64_t *out, unsigned int *count,
                   unsigned int cap, unsigned long long *stats, cudaStream_t s);
 void launch_narrow(bool fp64, const MeshDev &A, const MeshDev &B, const uint64_t *cand, int n, uint8_t *hit,
-                   double *seg, unsigned long long *stats, cudaStream_t s);
+                   double *seg, uint32_t *perm, unsigned long long *stats, cudaStream_t s);
 
 } // namespace sbg
