@@ -744,36 +744,99 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
 // Exact sides of one node whose member order matters: a member inside the interval (the reference's
 // sequential sum in member order decides), or an empty side (the split takes halves of the member order).
 // Run by the whole block; lists the members by triangle index, rewrites their state words and the children's
-// statistics. Rare.
+// statistics. `stage` is 2 x kStage doubles of shared memory. Symmetric inputs (an unjittered sphere: centres
+// exactly on the mean by symmetry) send most large nodes here.
+constexpr int kStage = 2048;
+static_assert(sizeof(NParam) * kTabNodes >= 2 * kStage * sizeof(double), "staging aliases the level table");
 __device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *state, const NParam &q, RNode &nd,
                              int *list, const int *__restrict__ posOf, int *warpSums, RunRec *runs, RStat *sAcc,
-                             int &sLeft, double &sSplit)
+                             int &sLeft, double &sSplit, double *stage)
 {
-    const int tid = threadIdx.x;
+    const unsigned full = 0xFFFFFFFFu;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, warps = blockDim.x >> 5;
     const int n = q.count;
     const bool amb = (__ldcg(&nd.flags) & 1) != 0;
     const int dir = __ldcg(&nd.dir), axis = q.axis;
     if (tid == 0)
         sLeft = 0;
-    int got = 0;
-    for (int b = 0; b < nt; b += blockDim.x) {
-        const int i = b + tid; // triangle index
-        const int pos = i < nt ? posOf[i] : 0;
-        const int m = (i < nt && st_node(__ldcg(&state[pos])) == id) ? 1 : 0;
-        int tot;
-        const int at = block_exclusive_scan(m, tot, warpSums);
-        if (m && got + at < n)
-            list[got + at] = pos;
-        got += tot;
-    }
-    __syncthreads();
-    if (amb) {
-        if (tid == 0) {
-            double s = 0.0;
-            for (int k = 0; k < n; ++k)
-                s = s + ord_to_dbl(rec[__ldcg(&list[dir ? n - 1 - k : k])].c[axis]);
-            sSplit = s / (double)(float)n;
+    // members by ascending triangle index: each warp scans one contiguous index range twice (count, then
+    // write from its offset), so no block barrier runs per chunk
+    {
+        const int per = (((nt + warps - 1) / warps) + 31) & ~31;
+        const int i0 = min(nt, w * per), i1 = min(nt, i0 + per);
+        int cnt = 0;
+#pragma unroll 4
+        for (int b = i0; b < i1; b += 32) {
+            const int i = b + lane;
+            const bool m = i < i1 && st_node(__ldcg(&state[posOf[i]])) == id;
+            cnt += __popc(__ballot_sync(full, m));
         }
+        if (lane == 0)
+            warpSums[w] = cnt;
+        __syncthreads();
+        int off = 0;
+        for (int k = 0; k < w; ++k)
+            off += warpSums[k];
+#pragma unroll 4
+        for (int b = i0; b < i1; b += 32) {
+            const int i = b + lane;
+            int pos = 0;
+            bool m = false;
+            if (i < i1) {
+                pos = posOf[i];
+                m = st_node(__ldcg(&state[pos])) == id;
+            }
+            const unsigned bal = __ballot_sync(full, m);
+            const int at = off + __popc(bal & ((1u << lane) - 1u));
+            if (m && at < n)
+                list[at] = pos;
+            off += __popc(bal);
+        }
+        __threadfence_block();
+        __syncthreads();
+    }
+    if (amb) {
+        // the reference's sum: sequential in member order. Warp 0's lane 0 adds one staged chunk while the
+        // other warps gather the next one into the other half of `stage`.
+        auto gather = [&](int c0, double *buf, int t0, int nthr) {
+            const int m = min(kStage, n - c0);
+            for (int k = t0; k < m; k += nthr) {
+                const int mp = c0 + k;
+                buf[k] = ord_to_dbl(rec[__ldcg(&list[dir ? n - 1 - mp : mp])].c[axis]);
+            }
+        };
+        gather(0, stage, tid, blockDim.x);
+        __syncthreads();
+        double s = 0.0;
+        for (int c0 = 0, j = 0; c0 < n; c0 += kStage, ++j) {
+            const double *cur = stage + (j & 1) * kStage;
+            if (w == 0) {
+                if (lane == 0) {
+                    const int m = min(kStage, n - c0);
+                    int k = 0;
+                    for (; k + 8 <= m; k += 8) {
+                        const double a0 = cur[k], a1 = cur[k + 1], a2 = cur[k + 2], a3 = cur[k + 3];
+                        const double a4 = cur[k + 4], a5 = cur[k + 5], a6 = cur[k + 6], a7 = cur[k + 7];
+                        s = s + a0;
+                        s = s + a1;
+                        s = s + a2;
+                        s = s + a3;
+                        s = s + a4;
+                        s = s + a5;
+                        s = s + a6;
+                        s = s + a7;
+                    }
+                    for (; k < m; ++k)
+                        s = s + cur[k];
+                }
+                __syncwarp();
+            } else if (c0 + kStage < n) {
+                gather(c0 + kStage, stage + ((j + 1) & 1) * kStage, tid - 32, blockDim.x - 32);
+            }
+            __syncthreads();
+        }
+        if (tid == 0)
+            sSplit = s / (double)(float)n;
         __syncthreads();
     }
     int myLeft = 0;
@@ -904,7 +967,7 @@ __global__ void __launch_bounds__(kElemThreads, 4)
                                  __ldcg(&nd.acc[1].count) == 0;
             if (flagged) // members of one level's nodes are disjoint: the node's leaf range is its list space
                 resolve_node(id, nt, rec, state, ld_nparam(&np[id]), nd, pool + __ldcg(&nd.begin), posOf, warpRuns,
-                             runs, sAcc, sLeft, sSplit);
+                             runs, sAcc, sLeft, sSplit, reinterpret_cast<double *>(tab.par));
             create_children(id, nodes, np, counters, terms, maxNodes, sc, &sLeft);
         }
         if (!grid_sync(gb))
