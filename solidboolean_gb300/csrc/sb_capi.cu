@@ -544,8 +544,10 @@ struct sb_boolean {
     cudaStream_t side = nullptr;     // second stream for preparing the two meshes concurrently
     cudaEvent_t sideDone = nullptr;
     bool evInit = false;
-    unsigned int *h_pinned = nullptr; // host mirror of small counters
+    char *mail = nullptr; // pinned mailbox: small reads [0, kMailRead), constant uploads after it
 };
+
+constexpr size_t kMailRead = kMailBytes - 64;
 
 namespace {
 
@@ -573,10 +575,53 @@ template <class Call> cudaError_t cub_run(sb_boolean *b, Call &&call)
     return call(b->cub.ptr, have);
 }
 
+// Small device-to-host reads through the boolean's pinned mailbox: queued on its stream, one synchronisation
+// for all of them, then copied out. (A pageable destination would take the driver's staging path, which
+// serialises the streams of concurrent booleans.)
+class Readback {
+public:
+    explicit Readback(sb_boolean *b) : b_(b) {}
+    cudaError_t add(void *dst, const void *src, size_t bytes)
+    {
+        const size_t at = (used_ + 7) & ~(size_t)7;
+        if (at + bytes > kMailRead || n_ == kItems)
+            return cudaErrorInvalidValue;
+        const cudaError_t e = cudaMemcpyAsync(b_->mail + at, src, bytes, cudaMemcpyDeviceToHost, b_->s);
+        if (e != cudaSuccess)
+            return e;
+        items_[n_++] = Item{dst, at, bytes};
+        used_ = at + bytes;
+        return cudaSuccess;
+    }
+    cudaError_t sync()
+    {
+        const cudaError_t e = cudaStreamSynchronize(b_->s);
+        if (e != cudaSuccess)
+            return e;
+        for (int i = 0; i < n_; ++i)
+            std::memcpy(items_[i].dst, b_->mail + items_[i].at, items_[i].bytes);
+        n_ = 0;
+        used_ = 0;
+        return cudaSuccess;
+    }
+
+private:
+    struct Item {
+        void *dst;
+        size_t at, bytes;
+    };
+    static constexpr int kItems = 16;
+    sb_boolean *b_;
+    Item items_[kItems];
+    int n_ = 0;
+    size_t used_ = 0;
+};
+
 sb_status read_back(sb_boolean *b, void *dst, const void *src, size_t bytes)
 {
-    SB_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->s));
-    SB_CUDA_CHECK(cudaStreamSynchronize(b->s));
+    Readback rb(b);
+    SB_CUDA_CHECK(rb.add(dst, src, bytes));
+    SB_CUDA_CHECK(rb.sync());
     return SB_OK;
 }
 
@@ -640,16 +685,16 @@ sb_status combine_impl(sb_boolean *b)
         (void)o_sel;
         SB_CUDA_CHECK(cudaMemsetAsync(d_count, 0, sizeof(unsigned int), s));
         SB_CUDA_CHECK(cudaMemsetAsync(d_stats, 0, 8 * sizeof(unsigned long long), s));
+        Readback rb(b);
         if (attempt == 0 && A.adj && B.adj) { // read with the candidate count below
-            SB_CUDA_CHECK(cudaMemcpyAsync(adjDup, A.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
-            SB_CUDA_CHECK(cudaMemcpyAsync(adjDup + 1, B.adjDup, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SB_CUDA_CHECK(rb.add(adjDup, A.adjDup, sizeof(int)));
+            SB_CUDA_CHECK(rb.add(adjDup + 1, B.adjDup, sizeof(int)));
         }
         launch_broad(fp64, A, B, reinterpret_cast<uint64_t *>(b->cand.as<char>() + o_raw), d_count, b->candCap,
                      d_stats, s);
         SB_CUDA_CHECK(cudaGetLastError());
-        sb_status r = read_back(b, &C, d_count, sizeof C);
-        if (r != SB_OK)
-            return r;
+        SB_CUDA_CHECK(rb.add(&C, d_count, sizeof C));
+        SB_CUDA_CHECK(rb.sync());
         if (C <= b->candCap)
             break;
         b->candCap = C + C / 4 + 1024;
@@ -818,11 +863,12 @@ sb_status combine_impl(sb_boolean *b)
         }));
         unsigned long long sTot = 0;
         int pTot = 0, tTot = 0, eTot = 0;
-        SB_CUDA_CHECK(cudaMemcpyAsync(&sTot, scratchOff + nFaces, sizeof sTot, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaMemcpyAsync(&pTot, ptOff + nFaces, sizeof pTot, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaMemcpyAsync(&tTot, triOff + nFaces, sizeof tTot, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaMemcpyAsync(&eTot, edgeOff + nFaces, sizeof eTot, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        Readback rb(b);
+        SB_CUDA_CHECK(rb.add(&sTot, scratchOff + nFaces, sizeof sTot));
+        SB_CUDA_CHECK(rb.add(&pTot, ptOff + nFaces, sizeof pTot));
+        SB_CUDA_CHECK(rb.add(&tTot, triOff + nFaces, sizeof tTot));
+        SB_CUDA_CHECK(rb.add(&eTot, edgeOff + nFaces, sizeof eTot));
+        SB_CUDA_CHECK(rb.sync());
         totals[0] = (long long)sTot;
         totals[1] = pTot;
         totals[2] = tTot;
@@ -871,7 +917,8 @@ sb_status combine_impl(sb_boolean *b)
 
     // ---------------- statuses ----------------
     int firstFail[3] = {INT_MAX, INT_MAX, INT_MAX};
-    SB_CUDA_CHECK(cudaMemcpyAsync(d_firstFail, firstFail, sizeof firstFail, cudaMemcpyHostToDevice, s));
+    // from the mailbox's constant area (three INT_MAX written when the boolean was created)
+    SB_CUDA_CHECK(cudaMemcpyAsync(d_firstFail, b->mail + kMailRead, sizeof firstFail, cudaMemcpyHostToDevice, s));
     if (nFaces > 0)
         SB_COUNT(k_face_status)<<<blocks(nFaces, 256), 256, 0, s>>>(nFaces, faceSide, faceStatus, d_firstFail);
 
@@ -979,12 +1026,15 @@ sb_status combine_impl(sb_boolean *b)
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceNtris, retriRank, nFaces + 1, s);
         }));
     int cnts[4] = {0, 0, 0, 0}; // uncutA, uncutB, retriA, retri total
-    SB_CUDA_CHECK(cudaMemcpyAsync(cnts, g.uncutRankA + nA, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 1, g.uncutRankB + nB, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 2, retriRank + FA, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(cnts + 3, retriRank + nFaces, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(firstFail, d_firstFail, sizeof firstFail, cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    {
+        Readback rb(b);
+        SB_CUDA_CHECK(rb.add(cnts, g.uncutRankA + nA, sizeof(int)));
+        SB_CUDA_CHECK(rb.add(cnts + 1, g.uncutRankB + nB, sizeof(int)));
+        SB_CUDA_CHECK(rb.add(cnts + 2, retriRank + FA, sizeof(int)));
+        SB_CUDA_CHECK(rb.add(cnts + 3, retriRank + nFaces, sizeof(int)));
+        SB_CUDA_CHECK(rb.add(firstFail, d_firstFail, sizeof firstFail));
+        SB_CUDA_CHECK(rb.sync());
+    }
     g.useAdj = adjDup[0] == 0 && adjDup[1] == 0;
     g.uncutA = cnts[0];
     g.uncutB = cnts[1];
@@ -1099,8 +1149,11 @@ sb_status combine_impl(sb_boolean *b)
     else if (firstFail[0] != INT_MAX || firstFail[1] != INT_MAX) {
         int f = firstFail[0] != INT_MAX ? firstFail[0] : firstFail[1];
         int code = 0;
-        SB_CUDA_CHECK(cudaMemcpyAsync(&code, faceStatus + f, sizeof code, cudaMemcpyDeviceToHost, s));
-        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        {
+            const sb_status r = read_back(b, &code, faceStatus + f, sizeof code);
+            if (r != SB_OK)
+                return r;
+        }
         status = code == 1 ? SB_FAIL_ATTACH : SB_FAIL_LINK;
     } else if (counters[kCntLoopVerts + 1] != 0)
         status = SB_FAIL_LOOP;
@@ -1109,6 +1162,7 @@ sb_status combine_impl(sb_boolean *b)
     if (status == SB_OK && nTri > 0) {
         // the three fetch compactions, one host read of their sizes
         int n[3] = {0, 0, 0};
+        Readback rb(b);
         for (int op = 0; op < 3; ++op) {
             int *fl = fFlag + op * ((size_t)nTri + 1), *rk = fRank + op * ((size_t)nTri + 1);
             SB_CUDA_CHECK(cudaMemsetAsync(fl + nTri, 0, sizeof(int), s));
@@ -1117,9 +1171,9 @@ sb_status combine_impl(sb_boolean *b)
                 return cub::DeviceScan::ExclusiveSum(tmp, bytes, fl, rk, nTri + 1, s);
             }));
             launch_fetch_write(g, op, fl, rk, fetchOut[op], s);
-            SB_CUDA_CHECK(cudaMemcpyAsync(n + op, rk + nTri, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SB_CUDA_CHECK(rb.add(n + op, rk + nTri, sizeof(int)));
         }
-        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+        SB_CUDA_CHECK(rb.sync());
         for (int op = 0; op < 3; ++op) {
             b->d_fetch[op] = fetchOut[op];
             b->nFetch[op] = (size_t)n[op];
@@ -1127,9 +1181,12 @@ sb_status combine_impl(sb_boolean *b)
     }
     SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));
     unsigned long long dstats[8];
-    SB_CUDA_CHECK(cudaMemcpyAsync(dstats, d_stats, sizeof dstats, cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaMemcpyAsync(counters, d_counters, sizeof counters, cudaMemcpyDeviceToHost, s));
-    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    {
+        Readback rb(b);
+        SB_CUDA_CHECK(rb.add(dstats, d_stats, sizeof dstats));
+        SB_CUDA_CHECK(rb.add(counters, d_counters, sizeof counters));
+        SB_CUDA_CHECK(rb.sync());
+    }
     SB_CUDA_CHECK(cudaGetLastError());
     {
         const sb_status r = rankResults();
@@ -1273,10 +1330,14 @@ static sb_status mesh_validate(sb_mesh *m, cudaStream_t s)
     d_bad = m->tmp.as<unsigned int>();
     SB_CUDA_CHECK(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), s));
     SB_COUNT(k_validate_tris)<<<blocks(3 * (size_t)m->d.nt, 256), 256, 0, s>>>(m->d.nt, m->d.nv, m->d.t, d_bad);
-    unsigned int bad = 0;
-    SB_CUDA_CHECK(cudaMemcpyAsync(&bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost, s));
+    // the mesh's pinned slot: ints [0, 12) hold the leaf-order status, the last one this flag
+    if (!m->rankCheck && !(m->rankCheck = pinned_slot_acquire())) {
+        set_last_error("no pinned host memory for the mesh");
+        return SB_ERR_CUDA;
+    }
+    SB_CUDA_CHECK(cudaMemcpyAsync(m->rankCheck + 15, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     SB_CUDA_CHECK(cudaStreamSynchronize(s));
-    if (bad) {
+    if (m->rankCheck[15]) {
         set_last_error("triangle index out of range");
         return SB_ERR_INVALID;
     }
@@ -1390,6 +1451,14 @@ sb_status sb_boolean_create(const sb_mesh *first, const sb_mesh *second, const s
         }
         b->s = (cudaStream_t)b->opts.stream;
         std::memset(&b->stats, 0, sizeof b->stats);
+        b->mail = pinned_mail_acquire();
+        if (!b->mail) {
+            delete b;
+            set_last_error("no pinned host memory for the boolean's mailbox");
+            return SB_ERR_CUDA;
+        }
+        const int big[3] = {INT_MAX, INT_MAX, INT_MAX};
+        std::memcpy(b->mail + kMailRead, big, sizeof big);
         *out = b;
         return SB_OK;
     });
@@ -1573,6 +1642,7 @@ void sb_boolean_destroy(sb_boolean *b)
         cudaStreamDestroy(b->side);
         cudaEventDestroy(b->sideDone);
     }
+    pinned_mail_release(b->mail);
     delete b;
 }
 
@@ -1640,11 +1710,35 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
         const int W = (int)std::max<int64_t>(1, std::min<int64_t>(workers > 0 ? workers : 8, (int64_t)n));
         std::atomic<size_t> next{0};
         std::vector<sb_status> setup(W, SB_OK);
-        // one worker: its own stream, a reusable pair of meshes and one boolean handle; pairs taken in turn
+        // the largest pair's inputs, for the workers' pinned staging buffers
+        size_t inMax = 0;
+        for (size_t i = 0; i < n; ++i)
+            inMax = std::max(inMax, 24 * (size_t)(v_off_a[i + 1] - v_off_a[i] + v_off_b[i + 1] - v_off_b[i]) +
+                                        12 * (size_t)(t_off_a[i + 1] - t_off_a[i] + t_off_b[i + 1] - t_off_b[i]) + 64);
+        // one worker: its own stream, a reusable pair of meshes and one boolean handle, a pinned staging buffer
+        // for uploads and result reads (pageable copies go through the driver's staging path, which
+        // serialises the workers' streams); pairs taken in turn
         auto pairs = [&](int w) {
             cudaStream_t s = nullptr;
             sb_mesh *ma = nullptr, *mb = nullptr;
             sb_boolean *x = nullptr;
+            char *stage = nullptr;
+            size_t stageBytes = 0;
+            auto stageFor = [&](size_t bytes) -> bool {
+                if (bytes <= stageBytes)
+                    return true;
+                if (stage)
+                    cudaFreeHost(stage);
+                stage = nullptr;
+                stageBytes = 0;
+                const size_t want = bytes + bytes / 4;
+                if (cudaMallocHost((void **)&stage, want) != cudaSuccess) {
+                    stage = nullptr;
+                    return false;
+                }
+                stageBytes = want;
+                return true;
+            };
             sb_status st = SB_OK;
             if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
                 st = SB_ERR_CUDA;
@@ -1656,31 +1750,45 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
             o.stream = s;
             if (st == SB_OK)
                 st = sb_boolean_create(ma, mb, &o, &x);
+            if (st == SB_OK && !stageFor(inMax))
+                st = SB_ERR_CUDA;
             setup[w] = st;
             for (size_t i = next++; st == SB_OK && i < n; i = next++) {
                 const int op = ops[i];
                 sb_status r = (op < SB_UNION || op > SB_INTERSECT) ? SB_ERR_INVALID : SB_OK;
+                const size_t nva = v_off_a[i + 1] - v_off_a[i], nta = t_off_a[i + 1] - t_off_a[i];
+                const size_t nvb = v_off_b[i + 1] - v_off_b[i], ntb = t_off_b[i + 1] - t_off_b[i];
+                // staged inputs: A's vertices, B's vertices, A's triangles, B's triangles
+                double *sva = reinterpret_cast<double *>(stage), *svb = sva + 3 * nva;
+                uint32_t *sta = reinterpret_cast<uint32_t *>(svb + 3 * nvb), *stb = sta + 3 * nta;
+                std::memcpy(sva, xyz_a + 3 * v_off_a[i], 24 * nva);
+                std::memcpy(svb, xyz_b + 3 * v_off_b[i], 24 * nvb);
+                std::memcpy(sta, tris_a + 3 * t_off_a[i], 12 * nta);
+                std::memcpy(stb, tris_b + 3 * t_off_b[i], 12 * ntb);
                 if (r == SB_OK)
-                    r = mesh_reset(ma, xyz_a + 3 * v_off_a[i], v_off_a[i + 1] - v_off_a[i], tris_a + 3 * t_off_a[i],
-                                   t_off_a[i + 1] - t_off_a[i], s);
+                    r = mesh_reset(ma, sva, nva, sta, nta, s);
                 if (r == SB_OK)
-                    r = mesh_reset(mb, xyz_b + 3 * v_off_b[i], v_off_b[i + 1] - v_off_b[i], tris_b + 3 * t_off_b[i],
-                                   t_off_b[i + 1] - t_off_b[i], s);
+                    r = mesh_reset(mb, svb, nvb, stb, ntb, s);
                 if (r == SB_OK)
                     r = sb_combine(x, nullptr);
                 statuses[i] = r;
                 if (keep && r == SB_OK) {
-                    size_t nv = 0, nt = 0;
-                    sb_status q = sb_result_vertices(x, nullptr, 0, &nv);
-                    if (q == SB_OK)
-                        q = sb_fetch(x, (sb_op)op, nullptr, 0, &nt);
+                    const size_t nv = x->nNewV, nt = x->nFetch[op];
+                    sb_status q = stageFor(24 * nv + 12 * nt + 64) ? SB_OK : SB_ERR_CUDA;
+                    double *rv = reinterpret_cast<double *>(stage);
+                    uint32_t *rt = reinterpret_cast<uint32_t *>(rv + 3 * nv);
+                    if (q == SB_OK && nv &&
+                        cudaMemcpyAsync(rv, x->d_newV, 24 * nv, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                        q = SB_ERR_CUDA;
+                    if (q == SB_OK && nt &&
+                        cudaMemcpyAsync(rt, x->d_fetch[op], 12 * nt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                        q = SB_ERR_CUDA;
+                    if (q == SB_OK && cudaStreamSynchronize(s) != cudaSuccess)
+                        q = SB_ERR_CUDA;
                     if (q == SB_OK) {
-                        keep->xyz[i].resize(3 * nv);
-                        keep->tris[i].resize(3 * nt);
-                        q = sb_result_vertices(x, keep->xyz[i].data(), nv, &nv);
+                        keep->xyz[i].assign(rv, rv + 3 * nv);
+                        keep->tris[i].assign(rt, rt + 3 * nt);
                     }
-                    if (q == SB_OK)
-                        q = sb_fetch(x, (sb_op)op, keep->tris[i].data(), nt, &nt);
                     if (q != SB_OK)
                         statuses[i] = q;
                 }
@@ -1691,6 +1799,8 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
             sb_mesh_destroy(mb);
             if (s)
                 cudaStreamDestroy(s);
+            if (stage)
+                cudaFreeHost(stage);
         };
         auto work = [&](int w) {
             try {

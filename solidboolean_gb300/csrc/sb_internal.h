@@ -87,6 +87,9 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank
 // sb_refrank.cu: position of each triangle in the reference tree's leaf order
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait);
 sb_status reference_rank_result(sb_mesh *m);
-int *pinned_slot_acquire();        // 16 ints of pinned host memory (null when none is left)
+int *pinned_slot_acquire();        // 16 ints of pinned host memory (null when none can be allocated)
 void pinned_slot_release(int *p);
+constexpr size_t kMailBytes = 1024; // a boolean's pinned mailbox for small device-to-host reads
+char *pinned_mail_acquire();
+void pinned_mail_release(char *p);
 } // namespace sbg

@@ -1399,38 +1399,49 @@ static sb_status rank_status(const int *chk)
     return SB_OK;
 }
 
-// Pinned 16-int slots for the leaf-order status of each mesh, carved from one block allocated once per
-// process: pinned allocations are slow and synchronising, and meshes come and go.
-static std::mutex g_pinMu;
-static int *g_pinBlock = nullptr;
-static std::vector<int *> g_pinFree;
-constexpr int kPinSlots = 4096;
-
-int *pinned_slot_acquire()
-{
-    std::lock_guard<std::mutex> lk(g_pinMu);
-    if (!g_pinBlock) {
-        if (cudaMallocHost((void **)&g_pinBlock, sizeof(int) * 16 * kPinSlots) != cudaSuccess) {
-            g_pinBlock = nullptr;
-            return nullptr;
+// Pinned host memory in fixed-size slots, carved from blocks that are allocated on demand and kept for the
+// process: pinned allocations are slow and synchronise the device, while meshes and booleans come and go.
+namespace {
+class PinnedPool {
+public:
+    PinnedPool(size_t slot, int perBlock) : slot_(slot), per_(perBlock) {}
+    void *acquire()
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (free_.empty()) {
+            char *blk = nullptr;
+            if (cudaMallocHost((void **)&blk, slot_ * (size_t)per_) != cudaSuccess)
+                return nullptr;
+            for (int i = per_ - 1; i >= 0; --i)
+                free_.push_back(blk + slot_ * (size_t)i);
         }
-        for (int i = kPinSlots - 1; i >= 0; --i)
-            g_pinFree.push_back(g_pinBlock + 16 * i);
+        void *p = free_.back();
+        free_.pop_back();
+        return p;
     }
-    if (g_pinFree.empty())
-        return nullptr;
-    int *p = g_pinFree.back();
-    g_pinFree.pop_back();
-    return p;
-}
+    void release(void *p)
+    {
+        if (!p)
+            return;
+        std::lock_guard<std::mutex> lk(mu_);
+        free_.push_back(static_cast<char *>(p));
+    }
 
-void pinned_slot_release(int *p)
-{
-    if (!p)
-        return;
-    std::lock_guard<std::mutex> lk(g_pinMu);
-    g_pinFree.push_back(p);
-}
+private:
+    size_t slot_;
+    int per_;
+    std::mutex mu_;
+    std::vector<char *> free_;
+};
+static_assert(kCtCount + sizeof(GridBar) / sizeof(int) <= 15, "the mesh's pinned slot keeps its last int for validation");
+PinnedPool g_slots(16 * sizeof(int), 4096);
+PinnedPool g_mail(kMailBytes, 256);
+} // namespace
+
+int *pinned_slot_acquire() { return static_cast<int *>(g_slots.acquire()); }
+void pinned_slot_release(int *p) { g_slots.release(p); }
+char *pinned_mail_acquire() { return static_cast<char *>(g_mail.acquire()); }
+void pinned_mail_release(char *p) { g_mail.release(p); }
 
 sb_status reference_rank_result(sb_mesh *m)
 {
@@ -1507,7 +1518,14 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     }
     SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
-    SB_CUDA_CHECK(cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem));
+    {
+        static std::once_flag smemOnce; // a per-call attribute set is a driver call every build
+        static cudaError_t smemErr = cudaSuccess;
+        std::call_once(smemOnce, [] {
+            smemErr = cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem);
+        });
+        SB_CUDA_CHECK(smemErr);
+    }
     // one block per terminal node; the count is known only on the device, so the grid covers every node record
     // that could be terminal and the surplus blocks return at once
     {
