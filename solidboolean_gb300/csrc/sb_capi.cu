@@ -196,6 +196,67 @@ __global__ void k_fill_u64(size_t n, uint64_t *a, uint64_t v)
         a[i] = v;
 }
 
+// Several buffers initialised by one launch (32-bit values, 64-bit values, index sequences): a small
+// boolean's setup is otherwise a dozen back-to-back launches of a few microseconds each.
+struct FillSeg {
+    void *p;
+    size_t n;
+    unsigned long long v;
+    int kind; // 0: 32-bit value, 1: 64-bit value, 2: a[i] = i
+};
+constexpr int kFillSegs = 12;
+struct FillList {
+    FillSeg seg[kFillSegs];
+    int count;
+};
+
+__global__ void k_fill_many(FillList f)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int k = 0; k < f.count; ++k) {
+        const FillSeg sg = f.seg[k];
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < sg.n; i += stride) {
+            if (sg.kind == 1)
+                static_cast<uint64_t *>(sg.p)[i] = sg.v;
+            else if (sg.kind == 2)
+                static_cast<int *>(sg.p)[i] = (int)i;
+            else
+                static_cast<int *>(sg.p)[i] = (int)(unsigned)sg.v;
+        }
+    }
+}
+
+class Fills {
+public:
+    explicit Fills(cudaStream_t s) : s_(s) { f_.count = 0; }
+    void i32(int *p, size_t n, int v) { add(p, n, (unsigned long long)(unsigned)v, 0); }
+    void u64(uint64_t *p, size_t n, uint64_t v) { add(p, n, v, 1); }
+    void iota(int *p, size_t n) { add(p, n, 0, 2); }
+    void launch()
+    {
+        if (f_.count == 0)
+            return;
+        const size_t b = std::min<size_t>((most_ + 255) / 256, 152 * 8);
+        SB_COUNT(k_fill_many)<<<(unsigned)std::max<size_t>(b, 1), 256, 0, s_>>>(f_);
+        f_.count = 0;
+        most_ = 0;
+    }
+
+private:
+    void add(void *p, size_t n, unsigned long long v, int kind)
+    {
+        if (n == 0)
+            return;
+        if (f_.count == kFillSegs)
+            launch();
+        f_.seg[f_.count++] = FillSeg{p, n, v, kind};
+        most_ = std::max(most_, n);
+    }
+    cudaStream_t s_;
+    FillList f_;
+    size_t most_ = 0;
+};
+
 // intersecting pair j: keys ordering its pairs inside the first mesh's face (by the second triangle's order
 // key) and inside the second mesh's face (by the first triangle's order key)
 __global__ void k_pair_keys(int K, const int *__restrict__ sel, const uint64_t *__restrict__ cand, int nB,
@@ -962,22 +1023,19 @@ sb_status combine_impl(sb_boolean *b)
     g.newSrc = (int *)(wb + o_nsrc);
     b->d_newSrc = g.newSrc;
     b->newBase = A.nv + B.nv;
-    SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldOwner, -1);
-    SB_COUNT(k_fill_i32)<<<blocks(weldCap, 256), 256, 0, s>>>(weldCap, g.weldMin, INT_MAX);
-    SB_CUDA_CHECK(cudaMemsetAsync(g.isFirst, 0, sizeof(int) * (nSeq + 1), s));
+    {
+        Fills fl(s);
+        fl.i32(g.weldOwner, weldCap, -1);
+        fl.i32(g.weldMin, weldCap, INT_MAX);
+        fl.i32(g.isFirst, nSeq + 1, 0);
+        fl.launch();
+    }
     launch_weld(g, s);
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, g.isFirst, g.firstRank, (int)nSeq + 1, s);
     }));
+    // the number of welded points is read with the arrangement's counts below (nothing before needs it)
     int nNew = 0;
-    {
-        sb_status r = read_back(b, &nNew, g.firstRank + nSeq, sizeof nNew);
-        if (r != SB_OK)
-            return r;
-    }
-    g.nNew = nNew;
-    st.new_points = (uint64_t)nNew;
-    const size_t nV = (size_t)A.nv + B.nv + nNew;
 
     // ---------------- arrangement ----------------
     Carve ca;
@@ -990,8 +1048,14 @@ sb_status combine_impl(sb_boolean *b)
     int *notA = (int *)(ab + o_nA), *notB = (int *)(ab + o_nB);
     g.uncutRankA = (int *)(ab + o_rA);
     g.uncutRankB = (int *)(ab + o_rB);
-    SB_CUDA_CHECK(cudaMemsetAsync(g.cutA, 0, sizeof(int) * (nA + 1), s));
-    SB_CUDA_CHECK(cudaMemsetAsync(g.cutB, 0, sizeof(int) * (nB + 1), s));
+    {
+        Fills fl(s);
+        fl.i32(g.cutA, nA + 1, 0);
+        fl.i32(g.cutB, nB + 1, 0);
+        fl.i32(notA, nA + 1, 0);
+        fl.i32(notB, nB + 1, 0);
+        fl.launch();
+    }
     launch_mark_cut(g, s);
     g.truncOcc = d_truncOcc;
     for (int side = 0; side < 2; ++side) {
@@ -1009,8 +1073,6 @@ sb_status combine_impl(sb_boolean *b)
         SB_COUNT(k_trunc_insert)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1);
         SB_COUNT(k_trunc_find)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1, d_truncOcc + side);
     }
-    SB_CUDA_CHECK(cudaMemsetAsync(notA, 0, sizeof(int) * (nA + 1), s));
-    SB_CUDA_CHECK(cudaMemsetAsync(notB, 0, sizeof(int) * (nB + 1), s));
     if (nA > 0)
         SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA, d_truncOcc);
     if (nB > 0)
@@ -1033,8 +1095,12 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(rb.add(cnts + 2, retriRank + FA, sizeof(int)));
         SB_CUDA_CHECK(rb.add(cnts + 3, retriRank + nFaces, sizeof(int)));
         SB_CUDA_CHECK(rb.add(firstFail, d_firstFail, sizeof firstFail));
+        SB_CUDA_CHECK(rb.add(&nNew, g.firstRank + nSeq, sizeof nNew));
         SB_CUDA_CHECK(rb.sync());
     }
+    g.nNew = nNew;
+    st.new_points = (uint64_t)nNew;
+    const size_t nV = (size_t)A.nv + B.nv + nNew;
     g.useAdj = adjDup[0] == 0 && adjDup[1] == 0;
     g.uncutA = cnts[0];
     g.uncutB = cnts[1];
@@ -1111,21 +1177,26 @@ sb_status combine_impl(sb_boolean *b)
     g.reps = (int *)(gb + o_rep);
     g.insideCount = (int *)(gb + o_ins);
 
-    SB_COUNT(k_fill_u64)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeKeys, kEmpty64);
-    SB_COUNT(k_fill_i32)<<<blocks(edgeCapH, 256), 256, 0, s>>>(edgeCapH, g.edgeVals, INT_MAX);
-    SB_CUDA_CHECK(cudaMemsetAsync(g.degree, 0, sizeof(int) * (nNew + 1), s));
-    launch_loops(g, s);
-    SB_COUNT(k_fill_u64)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysA, kEmpty64);
-    SB_COUNT(k_fill_u64)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heKeysB, kEmpty64);
-    SB_COUNT(k_fill_i32)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsA, INT_MAX);
-    SB_COUNT(k_fill_i32)<<<blocks(heCap, 256), 256, 0, s>>>(heCap, g.heValsB, INT_MAX);
-    if (nTri > 0) {
-        SB_COUNT(k_iota)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.parent);
-        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.seedMin, INT_MAX);
-        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.remMin, INT_MAX);
-        SB_COUNT(k_fill_i32)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, g.repOfRoot, -1);
-        SB_CUDA_CHECK(cudaMemsetAsync(g.insideCount, 0, sizeof(int) * (nTri + 1), s));
+    {
+        // the loop tables and every grouping table, in one launch before the loops
+        Fills fl(s);
+        fl.u64(g.edgeKeys, edgeCapH, kEmpty64);
+        fl.i32(g.edgeVals, edgeCapH, INT_MAX);
+        fl.i32(g.degree, (size_t)nNew + 1, 0);
+        fl.u64(g.heKeysA, heCap, kEmpty64);
+        fl.u64(g.heKeysB, heCap, kEmpty64);
+        fl.i32(g.heValsA, heCap, INT_MAX);
+        fl.i32(g.heValsB, heCap, INT_MAX);
+        if (nTri > 0) {
+            fl.iota(g.parent, nTri);
+            fl.i32(g.seedMin, nTri, INT_MAX);
+            fl.i32(g.remMin, nTri, INT_MAX);
+            fl.i32(g.repOfRoot, nTri, -1);
+            fl.i32(g.insideCount, (size_t)nTri + 1, 0);
+        }
+        fl.launch();
     }
+    launch_loops(g, s);
     launch_groups(g, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[5], s));
@@ -1161,8 +1232,6 @@ sb_status combine_impl(sb_boolean *b)
     // ---------------- fetch ----------------
     if (status == SB_OK && nTri > 0) {
         // the three fetch compactions, one host read of their sizes
-        int n[3] = {0, 0, 0};
-        Readback rb(b);
         for (int op = 0; op < 3; ++op) {
             int *fl = fFlag + op * ((size_t)nTri + 1), *rk = fRank + op * ((size_t)nTri + 1);
             SB_CUDA_CHECK(cudaMemsetAsync(fl + nTri, 0, sizeof(int), s));
@@ -1171,22 +1240,25 @@ sb_status combine_impl(sb_boolean *b)
                 return cub::DeviceScan::ExclusiveSum(tmp, bytes, fl, rk, nTri + 1, s);
             }));
             launch_fetch_write(g, op, fl, rk, fetchOut[op], s);
-            SB_CUDA_CHECK(rb.add(n + op, rk + nTri, sizeof(int)));
-        }
-        SB_CUDA_CHECK(rb.sync());
-        for (int op = 0; op < 3; ++op) {
-            b->d_fetch[op] = fetchOut[op];
-            b->nFetch[op] = (size_t)n[op];
         }
     }
     SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));
     unsigned long long dstats[8];
+    int nFetch[3] = {0, 0, 0}; // the three fetch sizes
     {
         Readback rb(b);
         SB_CUDA_CHECK(rb.add(dstats, d_stats, sizeof dstats));
         SB_CUDA_CHECK(rb.add(counters, d_counters, sizeof counters));
+        if (status == SB_OK && nTri > 0)
+            for (int op = 0; op < 3; ++op)
+                SB_CUDA_CHECK(rb.add(nFetch + op, fRank + op * ((size_t)nTri + 1) + nTri, sizeof(int)));
         SB_CUDA_CHECK(rb.sync());
     }
+    if (status == SB_OK && nTri > 0)
+        for (int op = 0; op < 3; ++op) {
+            b->d_fetch[op] = fetchOut[op];
+            b->nFetch[op] = (size_t)nFetch[op];
+        }
     SB_CUDA_CHECK(cudaGetLastError());
     {
         const sb_status r = rankResults();
