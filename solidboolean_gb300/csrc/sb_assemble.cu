@@ -727,42 +727,64 @@ __global__ void k_labels(int nTri, const int *__restrict__ root, const int *__re
 
 // fetch flags: union keeps outside of both, intersect inside of both, diff outside of the first and
 // inside of the second (reversed) (src/solidboolean.cpp:512-565)
+// Selection of the three results (src/solidboolean.cpp:512-570): union keeps the first mesh's outside and the
+// second's outside, intersect both insides, diff the first's outside and the second's inside with its
+// winding reversed. Flags of the three ops are laid out back to back, [op * (nTri + 1) + t], each run ending
+// in a zero, so one exclusive scan ranks all three: op k's output position is its rank minus the rank at the
+// start of its run.
+__device__ __forceinline__ int fetch_keep(int l, int mesh, int op)
+{
+    if (l < 0)
+        return 0;
+    if (op == 0)
+        return l == 0;
+    if (op == 2)
+        return l == 1;
+    return mesh == 0 ? (l == 0) : (l == 1);
+}
+
 __global__ void k_fetch_flags(int nTri, const int8_t *__restrict__ label, const int8_t *__restrict__ triMesh,
-                              int op, int *flag)
+                              int *flag)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > nTri)
+        return;
+    const size_t stride = (size_t)nTri + 1;
+    if (t == nTri) {
+        for (int op = 0; op < 3; ++op)
+            flag[op * stride + t] = 0;
+        return;
+    }
+    const int l = label[t], m = triMesh[t];
+    for (int op = 0; op < 3; ++op)
+        flag[op * stride + t] = fetch_keep(l, m, op);
+}
+
+__global__ void k_fetch_write(int nTri, const int *__restrict__ flag, const int *__restrict__ rank,
+                              const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh, uint32_t *out0,
+                              uint32_t *out1, uint32_t *out2)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nTri)
         return;
-    int l = label[t];
-    int keep;
-    if (l < 0)
-        keep = 0;
-    else if (op == 0)
-        keep = l == 0;
-    else if (op == 2)
-        keep = l == 1;
-    else
-        keep = triMesh[t] == 0 ? (l == 0) : (l == 1);
-    flag[t] = keep;
-}
-
-__global__ void k_fetch_write(int nTri, const int *__restrict__ flag, const int *__restrict__ rank,
-                              const uint32_t *__restrict__ newT, const int8_t *__restrict__ triMesh, int op,
-                              uint32_t *out)
-{
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nTri || !flag[t])
-        return;
+    const size_t stride = (size_t)nTri + 1;
     const uint32_t *v = newT + 3 * (size_t)t;
-    uint32_t *o = out + 3 * (size_t)rank[t];
-    if (op == 1 && triMesh[t] == 1) {
-        o[0] = v[2];
-        o[1] = v[1];
-        o[2] = v[0];
-    } else {
-        o[0] = v[0];
-        o[1] = v[1];
-        o[2] = v[2];
+    const uint32_t a = v[0], b = v[1], c = v[2];
+    const bool flip = triMesh[t] == 1;
+    uint32_t *outs[3] = {out0, out1, out2};
+    for (int op = 0; op < 3; ++op) {
+        if (!flag[op * stride + t])
+            continue;
+        uint32_t *o = outs[op] + 3 * (size_t)(rank[op * stride + t] - rank[op * stride]);
+        if (op == 1 && flip) {
+            o[0] = c;
+            o[1] = b;
+            o[2] = a;
+        } else {
+            o[0] = a;
+            o[1] = b;
+            o[2] = c;
+        }
     }
 }
 
@@ -963,22 +985,19 @@ void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t 
         }
 }
 
-void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s)
+void launch_fetch_flags(const AsmArgs &g, int *flag, cudaStream_t s)
 {
-    if (g.nTri > 0)
-        {
-            KTime kt("k_fetch_flags", s);
-            SB_COUNT(k_fetch_flags)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.label, g.triMesh, op, flag);
-        }
+    KTime kt("k_fetch_flags", s);
+    SB_COUNT(k_fetch_flags)<<<nb((size_t)g.nTri + 1, 256), 256, 0, s>>>(g.nTri, g.label, g.triMesh, flag);
 }
 
-void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s)
+void launch_fetch_write(const AsmArgs &g, const int *flag, const int *rank, uint32_t *const out[3], cudaStream_t s)
 {
-    if (g.nTri > 0)
-        {
-            KTime kt("k_fetch_write", s);
-            SB_COUNT(k_fetch_write)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, flag, rank, g.newT, g.triMesh, op, out);
-        }
+    if (g.nTri > 0) {
+        KTime kt("k_fetch_write", s);
+        SB_COUNT(k_fetch_write)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, flag, rank, g.newT, g.triMesh, out[0], out[1],
+                                                                 out[2]);
+    }
 }
 
 } // namespace sbg

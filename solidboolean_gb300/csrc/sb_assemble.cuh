@@ -77,7 +77,8 @@ void launch_groups(const AsmArgs &g, cudaStream_t s);
 void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s);
 // layout of the side-ray buffers for nRays rays (base null: bytes only)
 size_t side_layout(AsmArgs &g, int nRays, char *base);
-void launch_fetch_flags(const AsmArgs &g, int op, int *flag, cudaStream_t s);
-void launch_fetch_write(const AsmArgs &g, int op, const int *flag, const int *rank, uint32_t *out, cudaStream_t s);
+// the three results at once: flags [op * (nTri + 1) + t], one exclusive scan over all 3 (nTri + 1), writes
+void launch_fetch_flags(const AsmArgs &g, int *flag, cudaStream_t s);
+void launch_fetch_write(const AsmArgs &g, const int *flag, const int *rank, uint32_t *const out[3], cudaStream_t s);
 
 } // namespace sbg

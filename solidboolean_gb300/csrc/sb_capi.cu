@@ -1231,33 +1231,30 @@ sb_status combine_impl(sb_boolean *b)
 
     // ---------------- fetch ----------------
     if (status == SB_OK && nTri > 0) {
-        // the three fetch compactions, one host read of their sizes
-        for (int op = 0; op < 3; ++op) {
-            int *fl = fFlag + op * ((size_t)nTri + 1), *rk = fRank + op * ((size_t)nTri + 1);
-            SB_CUDA_CHECK(cudaMemsetAsync(fl + nTri, 0, sizeof(int), s));
-            launch_fetch_flags(g, op, fl, s);
-            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-                return cub::DeviceScan::ExclusiveSum(tmp, bytes, fl, rk, nTri + 1, s);
-            }));
-            launch_fetch_write(g, op, fl, rk, fetchOut[op], s);
-        }
+        // the three fetch compactions: one flag pass, one scan over the three runs, one write pass; their
+        // sizes are read with the final statistics
+        launch_fetch_flags(g, fFlag, s);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceScan::ExclusiveSum(tmp, bytes, fFlag, fRank, 3 * (nTri + 1), s);
+        }));
+        launch_fetch_write(g, fFlag, fRank, fetchOut, s);
     }
     SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));
     unsigned long long dstats[8];
-    int nFetch[3] = {0, 0, 0}; // the three fetch sizes
+    int runEnd[3] = {0, 0, 0}; // scan values where the three fetch runs end
     {
         Readback rb(b);
         SB_CUDA_CHECK(rb.add(dstats, d_stats, sizeof dstats));
         SB_CUDA_CHECK(rb.add(counters, d_counters, sizeof counters));
         if (status == SB_OK && nTri > 0)
             for (int op = 0; op < 3; ++op)
-                SB_CUDA_CHECK(rb.add(nFetch + op, fRank + op * ((size_t)nTri + 1) + nTri, sizeof(int)));
+                SB_CUDA_CHECK(rb.add(runEnd + op, fRank + op * ((size_t)nTri + 1) + nTri, sizeof(int)));
         SB_CUDA_CHECK(rb.sync());
     }
     if (status == SB_OK && nTri > 0)
         for (int op = 0; op < 3; ++op) {
             b->d_fetch[op] = fetchOut[op];
-            b->nFetch[op] = (size_t)nFetch[op];
+            b->nFetch[op] = (size_t)(runEnd[op] - (op > 0 ? runEnd[op - 1] : 0));
         }
     SB_CUDA_CHECK(cudaGetLastError());
     {

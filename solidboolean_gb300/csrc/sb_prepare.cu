@@ -16,9 +16,13 @@
 
 namespace sbg {
 
-__global__ void k_vertices_f32(int nv, const double *__restrict__ v, float4 *__restrict__ vf)
+// FP32 vertex copies; thread 0 also resets the 8 words of centre bounds that k_tri_boxes accumulates
+// (min keys at all ones, max keys and the rest at zero)
+__global__ void k_vertices_f32(int nv, const double *__restrict__ v, float4 *__restrict__ vf, unsigned int *bounds)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 8)
+        bounds[i] = i < 3 ? 0xFFFFFFFFu : 0u;
     if (i >= nv)
         return;
     vf[i] = make_float4(__double2float_rn(v[3 * i]), __double2float_rn(v[3 * i + 1]),
@@ -332,9 +336,7 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank
     int *idxIn = reinterpret_cast<int *>(tb + t_idx);
 
     const int BS = 256;
-    SB_COUNT(k_vertices_f32)<<<blocks_for(d.nv, BS), BS, 0, s>>>(d.nv, d.v, d.vf);
-    unsigned int initB[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
-    SB_CUDA_CHECK(cudaMemcpyAsync(bounds, initB, sizeof initB, cudaMemcpyHostToDevice, s));
+    SB_COUNT(k_vertices_f32)<<<blocks_for(std::max(d.nv, 8), BS), BS, 0, s>>>(d.nv, d.v, d.vf, bounds);
     SB_COUNT(k_tri_boxes)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.v, d.t, d.box64, d.box32, cen, bounds);
     SB_COUNT(k_morton)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tb + t_cub, sortBytes, keyIn, d.morton, idxIn, d.leafTri, nt, 0,

@@ -31,6 +31,7 @@
 // block per such node finishes its subtree in shared memory and writes the final positions.
 #include <algorithm>
 #include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <vector>
 
@@ -1312,42 +1313,103 @@ static int bit_length(int x)
     return b;
 }
 
-// Blocks of the cooperative large-node kernel: half of what can be resident at once (the two meshes of a
-// boolean are prepared concurrently, so two such grids must fit together), no more than the members need.
-// Cached per device.
 // Cooperative blocks of k_rr_top in flight per device. Cooperative grids launched from several streams at
 // once (two meshes of a boolean, batched booleans) must fit on the device together, or resident blocks of
-// one could wait at a grid barrier for blocks that cannot be scheduled; a launch therefore waits until its
-// blocks fit in the budget, and a host callback on its stream returns them when the kernel has finished.
+// one could wait at a grid barrier for blocks that cannot be scheduled. A launch takes its blocks from the
+// budget before it is issued and records an event after the kernel; blocks come back when a later launch
+// finds that event complete. A launch that does not fit waits for the oldest such event (its kernel is
+// already queued, so it finishes), never for a launch that has not been issued.
 struct CoopBudget {
     std::mutex mu;
-    std::condition_variable cv;
-    int capacity[256] = {0}, inFlight[256] = {0};
+    std::condition_variable cv; // a pending launch was held or cancelled
+    int capacity[256] = {0}, inFlight[256] = {0}, pending[256] = {0};
+    struct Held {
+        cudaEvent_t done;
+        int dev, blocks;
+    };
+    std::deque<Held> held;          // in launch order
+    std::vector<cudaEvent_t> spare; // events for reuse
 };
 static CoopBudget g_coop;
 
-struct CoopRelease {
-    int dev, blocks;
-};
-
-static void CUDART_CB coop_release(void *p)
+// with g_coop.mu held: return the blocks of every launch whose kernel has finished
+static void coop_reclaim_locked()
 {
-    CoopRelease *r = static_cast<CoopRelease *>(p);
-    {
-        std::lock_guard<std::mutex> lk(g_coop.mu);
-        g_coop.inFlight[r->dev] -= r->blocks;
+    for (auto it = g_coop.held.begin(); it != g_coop.held.end();) {
+        if (cudaEventQuery(it->done) == cudaSuccess) {
+            g_coop.inFlight[it->dev] -= it->blocks;
+            g_coop.spare.push_back(it->done);
+            it = g_coop.held.erase(it);
+        } else {
+            ++it;
+        }
     }
-    g_coop.cv.notify_all();
-    delete r;
 }
 
-static void coop_acquire(int dev, int blocks)
+static cudaError_t coop_acquire(int dev, int blocks)
 {
     std::unique_lock<std::mutex> lk(g_coop.mu);
-    g_coop.cv.wait(lk, [&] { return g_coop.inFlight[dev] + blocks <= g_coop.capacity[dev]; });
+    coop_reclaim_locked();
+    while (g_coop.inFlight[dev] + blocks > g_coop.capacity[dev]) {
+        if (g_coop.held.empty()) {
+            if (g_coop.pending[dev] == 0)
+                break; // nothing else holds blocks: a grid fits the device by construction
+            g_coop.cv.wait(lk); // launches between acquire and hold: each ends in a hold or a cancel
+            coop_reclaim_locked();
+            continue;
+        }
+        const cudaEvent_t oldest = g_coop.held.front().done;
+        lk.unlock();
+        const cudaError_t e = cudaEventSynchronize(oldest);
+        lk.lock();
+        if (e != cudaSuccess)
+            return e;
+        coop_reclaim_locked();
+    }
     g_coop.inFlight[dev] += blocks;
+    ++g_coop.pending[dev];
+    return cudaSuccess;
 }
 
+// after a successful cooperative launch on stream s: an event marks when its blocks are free again
+static cudaError_t coop_hold(int dev, int blocks, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> lk(g_coop.mu);
+    --g_coop.pending[dev];
+    g_coop.cv.notify_all();
+    cudaEvent_t e = nullptr;
+    if (!g_coop.spare.empty()) {
+        e = g_coop.spare.back();
+        g_coop.spare.pop_back();
+    } else {
+        const cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (ce != cudaSuccess) {
+            g_coop.inFlight[dev] -= blocks;
+            return ce;
+        }
+    }
+    const cudaError_t re = cudaEventRecord(e, s);
+    if (re != cudaSuccess) {
+        g_coop.spare.push_back(e);
+        g_coop.inFlight[dev] -= blocks;
+        return re;
+    }
+    g_coop.held.push_back(CoopBudget::Held{e, dev, blocks});
+    return cudaSuccess;
+}
+
+// a launch that failed returns its blocks at once
+static void coop_cancel(int dev, int blocks)
+{
+    std::lock_guard<std::mutex> lk(g_coop.mu);
+    g_coop.inFlight[dev] -= blocks;
+    --g_coop.pending[dev];
+    g_coop.cv.notify_all();
+}
+
+// Blocks of the cooperative large-node kernel: half of what can be resident at once (the two meshes of a
+// boolean are prepared concurrently, so two such grids must fit together), no more than the members need.
+// Cached per device.
 static int top_grid(int nt, int *devOut)
 {
     static int perSm[256], sms[256];
@@ -1502,19 +1564,18 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
         const int topBlocks = top_grid(nt, &dev);
         if (topBlocks <= 0)
             return SB_ERR_CUDA;
-        coop_acquire(dev, topBlocks);
+        SB_CUDA_CHECK(coop_acquire(dev, topBlocks));
         void *args[] = {(void *)&nt, (void *)&rec, (void *)&soa, (void *)&state, (void *)&np, (void *)&nodes, (void *)&counters,
                         (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar};
         count_launch();
         KTime kt("k_rr_top", s);
         const cudaError_t le =
             cudaLaunchCooperativeKernel((const void *)k_rr_top, dim3(topBlocks), dim3(kElemThreads), args, 0, s);
-        const cudaError_t ce = le == cudaSuccess ? cudaLaunchHostFunc(s, coop_release, new CoopRelease{dev, topBlocks})
-                                                 : le;
-        if (ce != cudaSuccess) {
-            coop_release(new CoopRelease{dev, topBlocks}); // no callback will return them
-            SB_CUDA_CHECK(ce);
+        if (le != cudaSuccess) {
+            coop_cancel(dev, topBlocks);
+            SB_CUDA_CHECK(le);
         }
+        SB_CUDA_CHECK(coop_hold(dev, topBlocks, s));
     }
     SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
