@@ -1540,18 +1540,16 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
     return guarded([&]() -> sb_status {
         sb_mesh *ma = const_cast<sb_mesh *>(b->first), *mb = const_cast<sb_mesh *>(b->second);
         if (!ma->prepared && !mb->prepared && ma != mb) {
-            // both meshes need preparing: the second one on a side stream from a helper thread, so the two
-            // latency-bound builds overlap; the main stream then waits for the side stream
+            // both meshes need preparing: the second one on a side stream, so the two latency-bound builds
+            // overlap on the device (issuing never blocks the host); the main stream then waits for the side
             if (!b->side) {
                 SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
                 SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->sideDone, cudaEventDisableTiming));
             }
             SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->s));
             SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
-            sb_status rb = SB_OK;
-            std::thread helper([&]() { rb = prepare_mesh(mb, b->opts.order, b->side, false); });
-            sb_status ra = prepare_mesh(ma, b->opts.order, b->s, false);
-            helper.join();
+            const sb_status ra = prepare_mesh(ma, b->opts.order, b->s, false);
+            const sb_status rb = ra == SB_OK ? prepare_mesh(mb, b->opts.order, b->side, false) : SB_OK;
             if (ra != SB_OK)
                 return ra;
             if (rb != SB_OK)
