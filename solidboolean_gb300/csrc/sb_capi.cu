@@ -1548,12 +1548,9 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
             }
             SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->s));
             SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
-            const sb_status ra = prepare_mesh(ma, b->opts.order, b->s, false);
-            const sb_status rb = ra == SB_OK ? prepare_mesh(mb, b->opts.order, b->side, false) : SB_OK;
-            if (ra != SB_OK)
-                return ra;
-            if (rb != SB_OK)
-                return rb;
+            const sb_status r = prepare_meshes(ma, b->s, mb, b->side, b->opts.order);
+            if (r != SB_OK)
+                return r;
             SB_CUDA_CHECK(cudaEventRecord(b->sideDone, b->side));
             SB_CUDA_CHECK(cudaStreamWaitEvent(b->s, b->sideDone, 0));
         }

@@ -84,6 +84,9 @@ namespace sbg {
 // With waitRank false the reference leaf order may still be running on m->aux when this returns: the caller
 // orders later work after m->auxJoin and calls reference_rank_result after a synchronisation past it.
 sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank = true);
+// both meshes of a boolean, each on its own stream, neither joining its leaf order; issued in the order that
+// starts the two leaf orders (the longer path) first
+sb_status prepare_meshes(sb_mesh *a, cudaStream_t sa, sb_mesh *b, cudaStream_t sb, int order_mode);
 // sb_refrank.cu: position of each triangle in the reference tree's leaf order
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait);
 sb_status reference_rank_result(sb_mesh *m);

@@ -261,14 +261,28 @@ __global__ void k_adj_find(int nt, const uint32_t *__restrict__ t, const uint64_
     }
 }
 
-sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank)
+// What the phases of one mesh's preparation pass on to each other.
+struct PrepState {
+    bool active = false; // the mesh has triangles and was not prepared
+    bool fork = false;   // the reference leaf order is built (on the mesh's second stream)
+    char *tb = nullptr;  // temporaries
+    size_t t_ak = 0, t_av = 0;
+    uint32_t adjCap = 0;
+    cudaStream_t s = nullptr;
+};
+
+// Phase 1: layout, FP32 vertices, triangle boxes, Morton codes and order; the second stream forks here.
+static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepState &ps)
 {
     MeshDev &d = m->d;
     const int nt = d.nt;
+    ps = PrepState{};
+    ps.s = s;
     if (nt <= 0) {
         m->prepared = true;
         return SB_OK;
     }
+    ps.active = true;
     // layout of the prepared arrays after the input arrays (v, t) already in m->buf
     Carve c;
     size_t o_v = c.take<double>((size_t)d.nv * 3);
@@ -344,6 +358,11 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank
     // The reference leaf order needs only the boxes and the Morton order: it runs on a second stream while
     // this one builds and refits the LBVH.
     const bool fork = order_mode == SB_ORDER_REFERENCE;
+    ps.fork = fork;
+    ps.tb = tb;
+    ps.t_ak = t_ak;
+    ps.t_av = t_av;
+    ps.adjCap = adjCap;
     if (fork) {
         if (!m->aux) {
             SB_CUDA_CHECK(cudaStreamCreateWithFlags(&m->aux, cudaStreamNonBlocking));
@@ -353,6 +372,32 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank
         SB_CUDA_CHECK(cudaEventRecord(m->auxFork, s));
         SB_CUDA_CHECK(cudaStreamWaitEvent(m->aux, m->auxFork, 0));
     }
+    return SB_OK;
+}
+
+// Phase 2: the reference leaf order, issued on the mesh's second stream (waits there for phase 1).
+static sb_status prepare_rank(sb_mesh *m, bool waitRank, PrepState &ps)
+{
+    if (!ps.active || !ps.fork)
+        return SB_OK;
+    m->d.rankValid = false;
+    const sb_status st = build_reference_rank(m, m->aux, waitRank);
+    SB_CUDA_CHECK(cudaEventRecord(m->auxJoin, m->aux));
+    return st;
+}
+
+// Phase 3: LBVH hierarchy and refit, input edge adjacency; with waitRank the main stream joins the leaf order.
+static sb_status prepare_end(sb_mesh *m, bool waitRank, PrepState &ps)
+{
+    if (!ps.active)
+        return SB_OK;
+    MeshDev &d = m->d;
+    const int nt = d.nt;
+    cudaStream_t s = ps.s;
+    char *tb = ps.tb;
+    const uint32_t adjCap = ps.adjCap;
+    const size_t t_ak = ps.t_ak, t_av = ps.t_av;
+    const int BS = 256;
     if (nt > 1) {
         SB_CUDA_CHECK(cudaMemsetAsync(d.parent, 0xFF, sizeof(int) * 2 * (size_t)nt, s));
         SB_CUDA_CHECK(cudaMemsetAsync(d.flags, 0, sizeof(int) * (size_t)(nt - 1), s));
@@ -374,17 +419,51 @@ sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank
         m->adjValid = true;
     }
     SB_CUDA_CHECK(cudaGetLastError());
-    d.rankValid = false;
-    if (fork) {
-        sb_status st = build_reference_rank(m, m->aux, waitRank);
-        SB_CUDA_CHECK(cudaEventRecord(m->auxJoin, m->aux));
-        if (waitRank)
-            SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
-        if (st != SB_OK)
-            return st;
-    }
+    if (ps.fork && waitRank)
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
+    if (!ps.fork)
+        d.rankValid = false;
     m->prepared = true;
     return SB_OK;
+}
+
+sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank)
+{
+    PrepState ps;
+    sb_status r = prepare_begin(m, order_mode, s, ps);
+    if (r != SB_OK || !ps.active)
+        return r;
+    if (waitRank) {
+        // the leaf-order build synchronises the host: issue the LBVH first
+        r = prepare_end(m, false, ps);
+        if (r == SB_OK)
+            r = prepare_rank(m, true, ps);
+        if (r == SB_OK && ps.fork)
+            SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
+        return r;
+    }
+    r = prepare_rank(m, false, ps);
+    if (r != SB_OK)
+        return r;
+    return prepare_end(m, false, ps);
+}
+
+sb_status prepare_meshes(sb_mesh *a, cudaStream_t sa, sb_mesh *b, cudaStream_t sb, int order_mode)
+{
+    // the leaf orders are the longer path: both are issued before either LBVH
+    PrepState pa, pb;
+    sb_status r = prepare_begin(a, order_mode, sa, pa);
+    if (r == SB_OK)
+        r = prepare_begin(b, order_mode, sb, pb);
+    if (r == SB_OK)
+        r = prepare_rank(a, false, pa);
+    if (r == SB_OK)
+        r = prepare_rank(b, false, pb);
+    if (r == SB_OK)
+        r = prepare_end(a, false, pa);
+    if (r == SB_OK)
+        r = prepare_end(b, false, pb);
+    return r;
 }
 
 } // namespace sbg
