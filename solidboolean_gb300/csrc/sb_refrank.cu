@@ -1033,10 +1033,11 @@ __device__ __forceinline__ void snode_init(SNode &n, int begin, int count)
 // about 55 KB: four blocks per SM
 constexpr size_t kSubSmem = sizeof(SNode) * kSubNodes + sizeof(int) * (6 * kSub + 1 + kSubThreads / 32);
 
-__global__ void __launch_bounds__(kSubThreads, 4)
-    k_rr_subtree(const int *__restrict__ terms, const RNode *__restrict__ gnodes, const int *__restrict__ sorted,
-                 const RRec *__restrict__ rec, const int *__restrict__ posOf, const int *__restrict__ leafTri,
-                 const int *__restrict__ scg, int *rank, int *counters)
+// One terminal node of the large-node phase (terms[t]), by the whole block.
+__device__ __forceinline__ void subtree_one(int t, const int *__restrict__ terms, const RNode *__restrict__ gnodes,
+                                            const int *__restrict__ sorted, const RRec *__restrict__ rec,
+                                            const int *__restrict__ posOf, const int *__restrict__ leafTri,
+                                            const int *__restrict__ scg, int *rank, int *counters)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     SNode *nodes = reinterpret_cast<SNode *>(smem);
@@ -1047,9 +1048,7 @@ __global__ void __launch_bounds__(kSubThreads, 4)
     int *warpSum = scan + kSub + 1;
     __shared__ int nNodes, lFirst, lLast, anyAmb, err;
     const int tid = threadIdx.x;
-    if ((int)blockIdx.x >= counters[kCtTerms])
-        return;
-    const RNode &g = gnodes[terms[blockIdx.x]];
+    const RNode &g = gnodes[terms[t]];
     const int base = g.begin, n = g.count, dir = g.dir;
     int sc[3] = {scg[0], scg[1], scg[2]};
     // perm holds Morton positions (record indices), in member order
@@ -1303,6 +1302,20 @@ __global__ void __launch_bounds__(kSubThreads, 4)
         rank[leafTri[perm[cur][p]]] = base + p;
 }
 
+// The terminal nodes, a block at a time: the count is known only on the device, so the grid is one resident
+// wave (or the largest possible count, if smaller) and every block strides over the list.
+__global__ void __launch_bounds__(kSubThreads, 4)
+    k_rr_subtree(const int *__restrict__ terms, const RNode *__restrict__ gnodes, const int *__restrict__ sorted,
+                 const RRec *__restrict__ rec, const int *__restrict__ posOf, const int *__restrict__ leafTri,
+                 const int *__restrict__ scg, int *rank, int *counters)
+{
+    const int nTerms = counters[kCtTerms];
+    for (int t = blockIdx.x; t < nTerms; t += gridDim.x) {
+        subtree_one(t, terms, gnodes, sorted, rec, posOf, leafTri, scg, rank, counters);
+        __syncthreads(); // shared memory is reused by the next node
+    }
+}
+
 static int bit_length(int x)
 {
     int b = 0;
@@ -1518,6 +1531,25 @@ sb_status reference_rank_result(sb_mesh *m)
     return st;
 }
 
+// one resident wave of k_rr_subtree blocks on the current device
+static int subtree_grid()
+{
+    static int grid = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0, sms = 0, per = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaFuncSetAttribute(k_rr_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubSmem) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rr_subtree, kSubThreads, kSubSmem) == cudaSuccess)
+            grid = std::max(1, sms * per);
+        else
+            grid = 1 << 20; // unknown: no cap (the list is still covered)
+    });
+    return grid;
+}
+
 sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
 {
     MeshDev &d = m->d;
@@ -1589,11 +1621,10 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
         });
         SB_CUDA_CHECK(smemErr);
     }
-    // one block per terminal node; the count is known only on the device, so the grid covers every node record
-    // that could be terminal and the surplus blocks return at once
+    // the terminal nodes, a resident wave of blocks striding over the device-side list
     {
         KTime kt("k_rr_subtree", s);
-        SB_COUNT(k_rr_subtree)<<<maxNodes, kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri,
+        SB_COUNT(k_rr_subtree)<<<std::min(maxNodes, subtree_grid()), kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri,
                                                                         scg, d.rank, counters);
     }
     // counters and barrier record to pinned host memory; read now, or by reference_rank_result once the
