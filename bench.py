@@ -187,8 +187,8 @@ def kernel_bytes(name: str, st: dict, na: int, nb: int, nva: int, nvb: int) -> f
 
 # DRAM bytes per launch (read + write) of the kernels captured with ncu on this workload; the figures and
 # the command are in profiles/kernels_pair_large_L7.txt
-MEASURED_TRAFFIC = {"k_rr_top": 32.85e6, "k_rr_subtree": 35.55e6, "k_faces": 14.53e6, "k_broad": 19.56e6,
-                    "k_union": 26.97e6}
+MEASURED_TRAFFIC = {"k_rr_top": 32.85e6, "k_rr_subtree": 35.58e6, "k_faces": 14.53e6, "k_broad": 19.56e6,
+                    "k_union": 26.97e6, "k_refit": 40.79e6}
 
 
 def rr_levels(n: int) -> int:
