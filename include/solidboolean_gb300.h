@@ -101,6 +101,10 @@ sb_status sb_mesh_create_device(const double *d_xyz, size_t nv, const uint32_t *
                                 const sb_options *opts, sb_mesh **out);
 /* Replace the vertex positions (same count, device pointer) without rebuilding the handle. */
 sb_status sb_mesh_update_vertices_device(sb_mesh *m, const double *d_xyz, const sb_options *opts);
+/* Builds the mesh's search structures (LBVH, the reference tree's leaf order, edge adjacency) on
+ * opts->stream and returns without waiting for them; sb_combine orders itself after the build, whatever its
+ * stream, and reports a failure of the build as its own status. (sb_combine prepares unprepared meshes
+ * itself, both at once.) */
 sb_status sb_mesh_prepare(sb_mesh *m, const sb_options *opts);
 void sb_mesh_destroy(sb_mesh *m);
 
@@ -167,6 +171,13 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
 sb_status sb_batch_result_size(const sb_batch *b, size_t i, size_t *n_vertices, size_t *n_triangles);
 sb_status sb_batch_result(const sb_batch *b, size_t i, double *xyz, uint32_t *tris);
 void sb_batch_destroy(sb_batch *b);
+
+/* No counterpart in the reference. Page-locked host memory from a cache kept by the library, for result
+ * buffers that sb_fetch / sb_result_vertices fill at DMA speed (a pageable destination is copied through the
+ * driver's staging buffers and, when freshly allocated, first faulted in page by page). sb_host_alloc returns
+ * SB_ERR_CUDA when no page-locked memory can be had; sb_host_free(NULL) does nothing. Thread-safe. */
+sb_status sb_host_alloc(size_t bytes, void **ptr);
+void sb_host_free(void *ptr);
 
 #ifdef __cplusplus
 }

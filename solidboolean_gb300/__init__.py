@@ -14,6 +14,7 @@ the built library or without a CUDA device raises.
 from __future__ import annotations
 
 import ctypes
+import weakref
 import os
 
 import numpy as np
@@ -31,7 +32,7 @@ EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_kernel
            "sb_mesh_create_device",
            "sb_mesh_update_vertices_device", "sb_mesh_prepare", "sb_mesh_destroy", "sb_boolean_create",
            "sb_combine", "sb_fetch", "sb_result_vertices", "sb_fetch_device", "sb_result_vertices_device",
-           "sb_debug_dump", "sb_boolean_destroy"]
+           "sb_debug_dump", "sb_boolean_destroy", "sb_host_alloc", "sb_host_free"]
 
 
 class Options(ctypes.Structure):
@@ -105,6 +106,10 @@ def lib() -> ctypes.CDLL:
     L.sb_batch_result.restype = st
     L.sb_batch_result.argtypes = [vp, sz, vp, vp]
     L.sb_batch_destroy.argtypes = [vp]
+    L.sb_host_alloc.restype = st
+    L.sb_host_alloc.argtypes = [sz, ctypes.POINTER(vp)]
+    L.sb_host_free.restype = None
+    L.sb_host_free.argtypes = [vp]
     L.sb_adjoint.restype = st
     L.sb_adjoint.argtypes = [vp, vp, vp, vp, vp]
     _lib = L
@@ -180,6 +185,21 @@ class SolidMesh:
             pass
 
 
+def _host_array(rows: int, cols: int, dtype) -> np.ndarray:
+    """A result array in page-locked memory from the library's cache (returned to it when the array is
+    collected), so result reads run at DMA speed; plain numpy memory when none can be had."""
+    nbytes = rows * cols * np.dtype(dtype).itemsize
+    if nbytes == 0:
+        return np.zeros((rows, cols), dtype=dtype)
+    L = lib()
+    ptr = ctypes.c_void_p()
+    if L.sb_host_alloc(nbytes, ctypes.byref(ptr)) != SB_OK or not ptr.value:
+        return np.zeros((rows, cols), dtype=dtype)
+    raw = (ctypes.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(raw, L.sb_host_free, ptr.value)
+    return np.frombuffer(raw, dtype=dtype).reshape(rows, cols)
+
+
 class SolidBoolean:
     """src/solidboolean.h:33-58"""
 
@@ -204,7 +224,7 @@ class SolidBoolean:
         L = lib()
         n = ctypes.c_size_t()
         _check(L.sb_fetch(self._handle(), op, None, 0, ctypes.byref(n)), "sb_fetch")
-        out = np.zeros((n.value, 3), dtype=np.uint32)
+        out = _host_array(n.value, 3, np.uint32)
         if n.value:
             _check(L.sb_fetch(self._handle(), op, out.ctypes.data, n.value, ctypes.byref(n)), "sb_fetch")
         return out
@@ -225,7 +245,7 @@ class SolidBoolean:
         L = lib()
         n = ctypes.c_size_t()
         _check(L.sb_result_vertices(self._handle(), None, 0, ctypes.byref(n)), "sb_result_vertices")
-        out = np.zeros((n.value, 3), dtype=np.float64)
+        out = _host_array(n.value, 3, np.float64)
         if n.value:
             _check(L.sb_result_vertices(self._handle(), out.ctypes.data, n.value, ctypes.byref(n)),
                    "sb_result_vertices")

@@ -11,6 +11,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <unordered_map>
 #include <thread>
 #include <string>
 #include <vector>
@@ -713,6 +714,10 @@ sb_status combine_impl(sb_boolean *b)
             SB_CUDA_CHECK(cudaEventCreate(&e));
         b->evInit = true;
     }
+    // the meshes may have been prepared on other streams
+    for (const sb_mesh *cm : {b->first, b->second})
+        if (cm->readyEv)
+            SB_CUDA_CHECK(cudaStreamWaitEvent(s, cm->readyEv, 0));
     SB_CUDA_CHECK(cudaEventRecord(b->ev[0], s));
 
     // small device block: [0..7] stats u64, [8..] counters, firstFail, scalars
@@ -1465,6 +1470,11 @@ sb_status sb_mesh_update_vertices_device(sb_mesh *m, const double *d_xyz, const 
     if (!m || (m->d.nv && !d_xyz))
         return SB_ERR_INVALID;
     cudaStream_t s = opts ? (cudaStream_t)opts->stream : nullptr;
+    {
+        const sb_status r = mesh_order_after(m, s); // a pending build may still read the vertices
+        if (r != SB_OK)
+            return r;
+    }
     if (m->d.nv)
         SB_CUDA_CHECK(cudaMemcpyAsync(m->d.v, d_xyz, sizeof(double) * 3 * m->d.nv, cudaMemcpyDeviceToDevice, s));
     m->prepared = false;
@@ -1480,7 +1490,8 @@ sb_status sb_mesh_prepare(sb_mesh *m, const sb_options *opts)
         sb_default_options(&o);
         if (opts)
             o = *opts;
-        return prepare_mesh(m, o.order, (cudaStream_t)o.stream);
+        // issued without waiting: sb_combine orders itself after the build and reports its status
+        return prepare_mesh(m, o.order, (cudaStream_t)o.stream, false);
     });
 }
 
@@ -1500,6 +1511,8 @@ void sb_mesh_destroy(sb_mesh *m)
         cudaEventDestroy(m->auxFork);
     if (m->auxJoin)
         cudaEventDestroy(m->auxJoin);
+    if (m->readyEv)
+        cudaEventDestroy(m->readyEv);
     delete m;
 }
 
@@ -1907,6 +1920,63 @@ sb_status sb_batch_result(const sb_batch *b, size_t i, double *xyz, uint32_t *tr
 }
 
 void sb_batch_destroy(sb_batch *b) { delete b; }
+
+// page-locked host blocks, cached by size (a block serves requests down to half its size)
+namespace {
+struct HostCache {
+    std::mutex mu;
+    std::multimap<size_t, void *> free;
+    std::unordered_map<void *, size_t> live;
+    size_t cached = 0;
+};
+HostCache g_host;
+constexpr size_t kHostCacheBytes = 2ull << 30;
+} // namespace
+
+sb_status sb_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr)
+        return SB_ERR_INVALID;
+    *ptr = nullptr;
+    const size_t want = std::max<size_t>(((bytes + 65535) >> 16) << 16, 65536);
+    {
+        std::lock_guard<std::mutex> lk(g_host.mu);
+        auto it = g_host.free.lower_bound(want);
+        if (it != g_host.free.end() && it->first <= 2 * want) {
+            *ptr = it->second;
+            g_host.live[it->second] = it->first;
+            g_host.cached -= it->first;
+            g_host.free.erase(it);
+            return SB_OK;
+        }
+    }
+    void *p = nullptr;
+    const cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMallocHost(result buffer)", __FILE__, __LINE__);
+    std::lock_guard<std::mutex> lk(g_host.mu);
+    g_host.live[p] = want;
+    *ptr = p;
+    return SB_OK;
+}
+
+void sb_host_free(void *ptr)
+{
+    if (!ptr)
+        return;
+    std::lock_guard<std::mutex> lk(g_host.mu);
+    auto it = g_host.live.find(ptr);
+    if (it == g_host.live.end())
+        return;
+    const size_t sz = it->second;
+    g_host.live.erase(it);
+    if (g_host.cached + sz <= kHostCacheBytes) {
+        g_host.free.insert({sz, ptr});
+        g_host.cached += sz;
+    } else {
+        cudaFreeHost(ptr);
+    }
+}
 
 sb_status sb_adjoint(sb_boolean *b, const double *d_grad_result, double *d_grad_first, double *d_grad_second,
                      void *stream)

@@ -69,6 +69,7 @@ struct sb_mesh {
     sbg::DevBuf rankTmp;           // reference leaf-order temporaries (built concurrently with the LBVH)
     cudaStream_t aux = nullptr;    // second stream of the preparation, created on first use
     cudaEvent_t auxFork = nullptr, auxJoin = nullptr;
+    cudaEvent_t readyEv = nullptr; // recorded after the last preparation's work on its own stream
     bool prepared = false;
     bool adjValid = false;         // adj / adjDup computed for the current triangles
     int *rankCheck = nullptr;      // pinned: the leaf-order build's counters, read once its stream is done
@@ -84,6 +85,9 @@ namespace sbg {
 // With waitRank false the reference leaf order may still be running on m->aux when this returns: the caller
 // orders later work after m->auxJoin and calls reference_rank_result after a synchronisation past it.
 sb_status prepare_mesh(sb_mesh *m, int order_mode, cudaStream_t s, bool waitRank = true);
+// orders work issued next on s after everything a previous preparation of m issued (its LBVH build on the
+// stream it was prepared on, and a leaf-order build still pending on the mesh's second stream); no host wait
+sb_status mesh_order_after(sb_mesh *m, cudaStream_t s);
 // both meshes of a boolean, each on its own stream, neither joining its leaf order; issued in the order that
 // starts the two leaf orders (the longer path) first
 sb_status prepare_meshes(sb_mesh *a, cudaStream_t sa, sb_mesh *b, cudaStream_t sb, int order_mode);

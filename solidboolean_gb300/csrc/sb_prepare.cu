@@ -271,6 +271,15 @@ struct PrepState {
     cudaStream_t s = nullptr;
 };
 
+sb_status mesh_order_after(sb_mesh *m, cudaStream_t s)
+{
+    if (m->rankPending && m->aux)
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
+    if (m->readyEv)
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->readyEv, 0));
+    return SB_OK;
+}
+
 // Phase 1: layout, FP32 vertices, triangle boxes, Morton codes and order; the second stream forks here.
 static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepState &ps)
 {
@@ -278,6 +287,12 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
     const int nt = d.nt;
     ps = PrepState{};
     ps.s = s;
+    {
+        // the buffers below may still be read by a previous preparation's work
+        const sb_status r = mesh_order_after(m, s);
+        if (r != SB_OK)
+            return r;
+    }
     if (nt <= 0) {
         m->prepared = true;
         return SB_OK;
@@ -423,6 +438,9 @@ static sb_status prepare_end(sb_mesh *m, bool waitRank, PrepState &ps)
         SB_CUDA_CHECK(cudaStreamWaitEvent(s, m->auxJoin, 0));
     if (!ps.fork)
         d.rankValid = false;
+    if (!m->readyEv)
+        SB_CUDA_CHECK(cudaEventCreateWithFlags(&m->readyEv, cudaEventDisableTiming));
+    SB_CUDA_CHECK(cudaEventRecord(m->readyEv, s));
     m->prepared = true;
     return SB_OK;
 }
