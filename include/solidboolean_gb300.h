@@ -148,8 +148,9 @@ sb_status sb_retriangulate_faces_noalloc(const double *d_corners, const int *d_s
  * Inputs are host arrays in CSR form: pair i's first mesh has the vertices xyz_a[3*v_off_a[i] ..
  * 3*v_off_a[i+1]) and the triangles tris_a[3*t_off_a[i] .. 3*t_off_a[i+1]) (vertex indices local to that
  * mesh); likewise the second mesh; ops[i] (an sb_op) names the result kept for the pair. statuses[i]
- * receives what sb_combine would return for the pair. Pairs run on `workers` concurrent streams (0: 8), each
- * with reusable handles. With out non-NULL the results (all result vertices, the op's triangles) are kept
+ * receives what sb_combine would return for the pair. Pairs run on `workers` concurrent streams (at most 64),
+ * each with reusable handles; workers <= 0 tunes the count: with at least 512 pairs, three runs of 64 pairs
+ * on 4, 8 and 16 workers (their results are kept like any other) pick the fastest for the rest, else 8. With out non-NULL the results (all result vertices, the op's triangles) are kept
  * for sb_batch_result_size / sb_batch_result; with out NULL only the statuses are produced. The return value
  * reports failures of the batch itself (invalid arguments, stream or handle creation). */
 /* No counterpart in the reference. Adjoint of the last sb_combine with its combinatorics held fixed: given

@@ -300,7 +300,7 @@ OP_CODES = {"union": SB_UNION, "diff": SB_DIFF, "intersect": SB_INTERSECT}
 
 
 def batch_combine(pairs, weld_factor: int = 100000, precision: str = "filtered", order: str = "reference",
-                  workers: int = 8, keep: bool = True):
+                  workers: int = 0, keep: bool = True):
     """Many independent booleans in one call (sb_batch_combine). pairs: sequence of (va, fa, vb, fb, op) with
     op in "union" / "diff" / "intersect". Returns (statuses, results): statuses an int32 array of per-pair
     sb_combine codes; results (when keep) a list of (result vertices, the op's triangles) per pair, empty

@@ -6,6 +6,7 @@
 // handful of counts that size the next stage (candidates, intersecting pairs, faces, per-face totals).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <climits>
 #include <cstring>
 #include <map>
@@ -1764,6 +1765,9 @@ sb_status mesh_reset(sb_mesh *m, const double *xyz, size_t nv, const uint32_t *t
 
 extern "C" {
 
+constexpr int kMaxWorkers = 64;
+constexpr size_t kTuneChunk = 64; // pairs per calibration run of the worker-count autotuner
+
 sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_a, const uint32_t *tris_a,
                            const uint64_t *t_off_a, const double *xyz_b, const uint64_t *v_off_b,
                            const uint32_t *tris_b, const uint64_t *t_off_b, const int32_t *ops,
@@ -1784,81 +1788,108 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
             keep->xyz.resize(n);
             keep->tris.resize(n);
         }
-        const int W = (int)std::max<int64_t>(1, std::min<int64_t>(workers > 0 ? workers : 8, (int64_t)n));
+        // pairs [next, end) go to the workers of the current run
         std::atomic<size_t> next{0};
-        std::vector<sb_status> setup(W, SB_OK);
+        size_t end = n;
+        std::vector<sb_status> setup(kMaxWorkers, SB_OK);
         // the largest pair's inputs, for the workers' pinned staging buffers
         size_t inMax = 0;
         for (size_t i = 0; i < n; ++i)
             inMax = std::max(inMax, 24 * (size_t)(v_off_a[i + 1] - v_off_a[i] + v_off_b[i + 1] - v_off_b[i]) +
                                         12 * (size_t)(t_off_a[i + 1] - t_off_a[i] + t_off_b[i + 1] - t_off_b[i]) + 64);
-        // one worker: its own stream, a reusable pair of meshes and one boolean handle, a pinned staging buffer
-        // for uploads and result reads (pageable copies go through the driver's staging path, which
-        // serialises the workers' streams); pairs taken in turn
-        auto pairs = [&](int w) {
+        // a worker's state lives across the runs of one call (the autotuner's calibration runs and the main
+        // run): a non-blocking stream, a reusable pair of meshes and one boolean handle, a pinned staging
+        // buffer for uploads and result reads (pageable copies go through the driver's staging path, which
+        // serialises the workers' streams)
+        struct Worker {
             cudaStream_t s = nullptr;
             sb_mesh *ma = nullptr, *mb = nullptr;
             sb_boolean *x = nullptr;
             char *stage = nullptr;
             size_t stageBytes = 0;
+            bool ready = false;
+        };
+        std::vector<Worker> wk(kMaxWorkers);
+        struct WorkersGone { // releases every worker's state however the call ends
+            std::vector<Worker> &wk;
+            ~WorkersGone()
+            {
+                for (Worker &k : wk) {
+                    if (k.x)
+                        sb_boolean_destroy(k.x);
+                    sb_mesh_destroy(k.ma);
+                    sb_mesh_destroy(k.mb);
+                    if (k.s)
+                        cudaStreamDestroy(k.s);
+                    if (k.stage)
+                        cudaFreeHost(k.stage);
+                }
+            }
+        } gone{wk};
+        auto pairs = [&](int w) {
+            Worker &k = wk[w];
             auto stageFor = [&](size_t bytes) -> bool {
-                if (bytes <= stageBytes)
+                if (bytes <= k.stageBytes)
                     return true;
-                if (stage)
-                    cudaFreeHost(stage);
-                stage = nullptr;
-                stageBytes = 0;
+                if (k.stage)
+                    cudaFreeHost(k.stage);
+                k.stage = nullptr;
+                k.stageBytes = 0;
                 const size_t want = bytes + bytes / 4;
-                if (cudaMallocHost((void **)&stage, want) != cudaSuccess) {
-                    stage = nullptr;
+                if (cudaMallocHost((void **)&k.stage, want) != cudaSuccess) {
+                    k.stage = nullptr;
                     return false;
                 }
-                stageBytes = want;
+                k.stageBytes = want;
                 return true;
             };
             sb_status st = SB_OK;
-            if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
-                st = SB_ERR_CUDA;
-            if (st == SB_OK)
-                st = mesh_alloc(0, 0, &ma);
-            if (st == SB_OK)
-                st = mesh_alloc(0, 0, &mb);
-            sb_options o = base;
-            o.stream = s;
-            if (st == SB_OK)
-                st = sb_boolean_create(ma, mb, &o, &x);
-            if (st == SB_OK && !stageFor(inMax))
-                st = SB_ERR_CUDA;
+            if (!k.ready) {
+                if (cudaStreamCreateWithFlags(&k.s, cudaStreamNonBlocking) != cudaSuccess)
+                    st = SB_ERR_CUDA;
+                if (st == SB_OK)
+                    st = mesh_alloc(0, 0, &k.ma);
+                if (st == SB_OK)
+                    st = mesh_alloc(0, 0, &k.mb);
+                sb_options o = base;
+                o.stream = k.s;
+                if (st == SB_OK)
+                    st = sb_boolean_create(k.ma, k.mb, &o, &k.x);
+                if (st == SB_OK && !stageFor(inMax))
+                    st = SB_ERR_CUDA;
+                k.ready = st == SB_OK;
+            }
             setup[w] = st;
-            for (size_t i = next++; st == SB_OK && i < n; i = next++) {
+            cudaStream_t s = k.s;
+            for (size_t i = next++; st == SB_OK && i < end; i = next++) {
                 const int op = ops[i];
                 sb_status r = (op < SB_UNION || op > SB_INTERSECT) ? SB_ERR_INVALID : SB_OK;
                 const size_t nva = v_off_a[i + 1] - v_off_a[i], nta = t_off_a[i + 1] - t_off_a[i];
                 const size_t nvb = v_off_b[i + 1] - v_off_b[i], ntb = t_off_b[i + 1] - t_off_b[i];
                 // staged inputs: A's vertices, B's vertices, A's triangles, B's triangles
-                double *sva = reinterpret_cast<double *>(stage), *svb = sva + 3 * nva;
+                double *sva = reinterpret_cast<double *>(k.stage), *svb = sva + 3 * nva;
                 uint32_t *sta = reinterpret_cast<uint32_t *>(svb + 3 * nvb), *stb = sta + 3 * nta;
                 std::memcpy(sva, xyz_a + 3 * v_off_a[i], 24 * nva);
                 std::memcpy(svb, xyz_b + 3 * v_off_b[i], 24 * nvb);
                 std::memcpy(sta, tris_a + 3 * t_off_a[i], 12 * nta);
                 std::memcpy(stb, tris_b + 3 * t_off_b[i], 12 * ntb);
                 if (r == SB_OK)
-                    r = mesh_reset(ma, sva, nva, sta, nta, s);
+                    r = mesh_reset(k.ma, sva, nva, sta, nta, s);
                 if (r == SB_OK)
-                    r = mesh_reset(mb, svb, nvb, stb, ntb, s);
+                    r = mesh_reset(k.mb, svb, nvb, stb, ntb, s);
                 if (r == SB_OK)
-                    r = sb_combine(x, nullptr);
+                    r = sb_combine(k.x, nullptr);
                 statuses[i] = r;
                 if (keep && r == SB_OK) {
-                    const size_t nv = x->nNewV, nt = x->nFetch[op];
+                    const size_t nv = k.x->nNewV, nt = k.x->nFetch[op];
                     sb_status q = stageFor(24 * nv + 12 * nt + 64) ? SB_OK : SB_ERR_CUDA;
-                    double *rv = reinterpret_cast<double *>(stage);
+                    double *rv = reinterpret_cast<double *>(k.stage);
                     uint32_t *rt = reinterpret_cast<uint32_t *>(rv + 3 * nv);
                     if (q == SB_OK && nv &&
-                        cudaMemcpyAsync(rv, x->d_newV, 24 * nv, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                        cudaMemcpyAsync(rv, k.x->d_newV, 24 * nv, cudaMemcpyDeviceToHost, s) != cudaSuccess)
                         q = SB_ERR_CUDA;
                     if (q == SB_OK && nt &&
-                        cudaMemcpyAsync(rt, x->d_fetch[op], 12 * nt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                        cudaMemcpyAsync(rt, k.x->d_fetch[op], 12 * nt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
                         q = SB_ERR_CUDA;
                     if (q == SB_OK && cudaStreamSynchronize(s) != cudaSuccess)
                         q = SB_ERR_CUDA;
@@ -1870,14 +1901,6 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
                         statuses[i] = q;
                 }
             }
-            if (x)
-                sb_boolean_destroy(x);
-            sb_mesh_destroy(ma);
-            sb_mesh_destroy(mb);
-            if (s)
-                cudaStreamDestroy(s);
-            if (stage)
-                cudaFreeHost(stage);
         };
         auto work = [&](int w) {
             try {
@@ -1886,15 +1909,46 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
                 setup[w] = SB_ERR_INVALID;
             }
         };
-        std::vector<std::thread> pool;
-        for (int w = 1; w < W; ++w)
-            pool.emplace_back(work, w);
-        work(0);
-        for (auto &t : pool)
-            t.join();
-        for (int w = 0; w < W; ++w)
-            if (setup[w] != SB_OK)
-                return setup[w];
+        // one run: W workers over pairs [begin, stop)
+        auto run = [&](size_t begin, size_t stop, int W) -> sb_status {
+            next = begin;
+            end = stop;
+            std::vector<std::thread> pool;
+            for (int w = 1; w < W; ++w)
+                pool.emplace_back(work, w);
+            work(0);
+            for (auto &t : pool)
+                t.join();
+            for (int w = 0; w < W; ++w)
+                if (setup[w] != SB_OK)
+                    return setup[w];
+            return SB_OK;
+        };
+        size_t done = 0;
+        int W = workers > 0 ? std::min(workers, kMaxWorkers) : 8;
+        if (workers <= 0 && n >= 8 * kTuneChunk) {
+            // autotune: successive chunks of pairs (kept as results) on each candidate worker count, timed on
+            // the host; the rest runs with the fastest
+            double best = 0.0;
+            for (int cand : {4, 8, 16}) {
+                const auto t0 = std::chrono::steady_clock::now();
+                const sb_status r = run(done, done + kTuneChunk, cand);
+                const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+                if (r != SB_OK)
+                    return r;
+                done += kTuneChunk;
+                if (best == 0.0 || dt < best) {
+                    best = dt;
+                    W = cand;
+                }
+            }
+        }
+        W = (int)std::max<int64_t>(1, std::min<int64_t>(W, (int64_t)(n - done)));
+        if (done < n) {
+            const sb_status r = run(done, n, W);
+            if (r != SB_OK)
+                return r;
+        }
         if (out)
             *out = keep.release();
         return SB_OK;
