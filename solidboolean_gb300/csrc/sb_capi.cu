@@ -261,13 +261,15 @@ private:
 
 // intersecting pair j: keys ordering its pairs inside the first mesh's face (by the second triangle's order
 // key) and inside the second mesh's face (by the first triangle's order key)
-__global__ void k_pair_keys(int K, const int *__restrict__ sel, const uint64_t *__restrict__ cand, int nB,
-                            const int *__restrict__ rankA, const int *__restrict__ rankB,
-                            const double *__restrict__ seg, const uint32_t *__restrict__ perm, uint64_t *keyA,
-                            uint64_t *keyB, int *val, double *segK, uint32_t *pairAB, uint32_t *pairPerm)
+// K: the number of intersecting pairs, or a bound on it with the count itself in dK (device memory)
+__global__ void k_pair_keys(int K, const unsigned int *dK, const int *__restrict__ sel,
+                            const uint64_t *__restrict__ cand, int nB, const int *__restrict__ rankA,
+                            const int *__restrict__ rankB, const double *__restrict__ seg,
+                            const uint32_t *__restrict__ perm, uint64_t *keyA, uint64_t *keyB, int *val,
+                            double *segK, uint32_t *pairAB, uint32_t *pairPerm)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= K)
+    if (j >= (dK ? (int)*dK : K))
         return;
     int idx = sel[j];
     uint64_t key = cand[idx];
@@ -306,10 +308,12 @@ union GroupSmem {
 };
 
 __global__ void __launch_bounds__(kGroupThreads)
-    k_face_group(int K, const uint64_t *__restrict__ keyA, const uint64_t *__restrict__ keyB,
-                 const int *__restrict__ val, int orderBitsA, int orderBitsB, int endBitA, int endBitB,
-                 int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB, unsigned int *runCount)
+    k_face_group(int Kin, const unsigned int *dK, const uint64_t *__restrict__ keyA,
+                 const uint64_t *__restrict__ keyB, const int *__restrict__ val, int orderBitsA, int orderBitsB,
+                 int endBitA, int endBitB, int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB,
+                 unsigned int *runCount)
 {
+    const int K = dK ? (int)*dK : Kin; // with dK, Kin bounds it (both at most kGroupMax)
     extern __shared__ __align__(16) unsigned char smemRaw[];
     GroupSmem &sm = *reinterpret_cast<GroupSmem *>(smemRaw);
     __shared__ int warpSums[kGroupThreads / 32];
@@ -796,26 +800,29 @@ sb_status combine_impl(sb_boolean *b)
             return cub::DeviceSelect::Flagged(tmp, bytes, thrust::counting_iterator<int>(0), hit, sel,
                                               d_count + 1, (int)C, s);
         }));
+    // With few candidates the intersecting pairs fit the one-block grouping whatever their number: their count
+    // stays on the device until the faces are counted, which saves a host round trip on small booleans.
     unsigned int K = 0;
-    if (C > 0) {
+    const bool deferK = C > 0 && C <= (unsigned int)kGroupMax;
+    if (C > 0 && !deferK) {
         sb_status r = read_back(b, &K, d_count + 1, sizeof K);
         if (r != SB_OK)
             return r;
     }
-    b->K = (int)K;
-    st.intersecting_pairs = K;
+    const unsigned int Kcap = deferK ? C : K; // buffer sizes and grids
+    const unsigned int *dK = deferK ? d_count + 1 : nullptr;
     SB_CUDA_CHECK(cudaEventRecord(b->ev[2], s));
 
     // ---------------- face lists ----------------
     Carve ci;
-    size_t o_keyA = ci.take<uint64_t>(K + 1), o_keyB = ci.take<uint64_t>(K + 1);
-    size_t o_keyAs = ci.take<uint64_t>(K + 1), o_keyBs = ci.take<uint64_t>(K + 1);
-    size_t o_val = ci.take<int>(K + 1), o_pidx = ci.take<int>(2 * (size_t)K + 2);
-    size_t o_segK = ci.take<double>(6 * (size_t)K + 6), o_ab = ci.take<uint32_t>(2 * (size_t)K + 2);
-    size_t o_pp = ci.take<uint32_t>((size_t)K + 1);
-    size_t o_hiA = ci.take<int>(K + 1), o_hiB = ci.take<int>(K + 1);
-    size_t o_uqA = ci.take<int>(K + 1), o_uqB = ci.take<int>(K + 1);
-    size_t o_ctA = ci.take<int>(K + 1), o_ctB = ci.take<int>(K + 1);
+    size_t o_keyA = ci.take<uint64_t>(Kcap + 1), o_keyB = ci.take<uint64_t>(Kcap + 1);
+    size_t o_keyAs = ci.take<uint64_t>(Kcap + 1), o_keyBs = ci.take<uint64_t>(Kcap + 1);
+    size_t o_val = ci.take<int>(Kcap + 1), o_pidx = ci.take<int>(2 * (size_t)Kcap + 2);
+    size_t o_segK = ci.take<double>(6 * (size_t)Kcap + 6), o_ab = ci.take<uint32_t>(2 * (size_t)Kcap + 2);
+    size_t o_pp = ci.take<uint32_t>((size_t)Kcap + 1);
+    size_t o_hiA = ci.take<int>(Kcap + 1), o_hiB = ci.take<int>(Kcap + 1);
+    size_t o_uqA = ci.take<int>(Kcap + 1), o_uqB = ci.take<int>(Kcap + 1);
+    size_t o_ctA = ci.take<int>(Kcap + 1), o_ctB = ci.take<int>(Kcap + 1);
     SB_CUDA_CHECK(b->isect.ensure(ci.off));
     char *ib = b->isect.as<char>();
     uint64_t *keyA = (uint64_t *)(ib + o_keyA), *keyB = (uint64_t *)(ib + o_keyB);
@@ -844,11 +851,11 @@ sb_status combine_impl(sb_boolean *b)
     };
     const bool useRank = b->opts.order == SB_ORDER_REFERENCE && A.rankValid && B.rankValid;
     int FA = 0, FB = 0;
-    if (K > 0) {
-        SB_COUNT(k_pair_keys)<<<blocks(K, 256), 256, 0, s>>>((int)K, sel, candSorted, nB, useRank ? A.rank : nullptr,
-                                                   useRank ? B.rank : nullptr, seg, perm, keyA, keyB, val, segK,
-                                                   pairAB, pairPerm);
-        if (K <= (unsigned int)kGroupMax) {
+    if (Kcap > 0) {
+        SB_COUNT(k_pair_keys)<<<blocks(Kcap, 256), 256, 0, s>>>((int)Kcap, dK, sel, candSorted, nB,
+                                                      useRank ? A.rank : nullptr, useRank ? B.rank : nullptr, seg,
+                                                      perm, keyA, keyB, val, segK, pairAB, pairPerm);
+        if (Kcap <= (unsigned int)kGroupMax) {
             const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
             const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
             static std::once_flag smemOnce;
@@ -856,7 +863,7 @@ sb_status combine_impl(sb_boolean *b)
                 cudaFuncSetAttribute(k_face_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupSmem));
             });
             SB_COUNT(k_face_group)<<<2, kGroupThreads, sizeof(GroupSmem), s>>>(
-                (int)K, keyA, keyB, val, obA, obB, ebA, ebB, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
+                (int)Kcap, dK, keyA, keyB, val, obA, obB, ebA, ebB, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
         } else {
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
                 return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
@@ -874,12 +881,16 @@ sb_status combine_impl(sb_boolean *b)
             }));
         }
         unsigned int runs[2];
-        sb_status r = read_back(b, runs, d_count + 2, sizeof runs);
-        if (r != SB_OK)
-            return r;
+        Readback rb(b);
+        SB_CUDA_CHECK(rb.add(runs, d_count + 2, sizeof runs));
+        if (deferK)
+            SB_CUDA_CHECK(rb.add(&K, d_count + 1, sizeof K));
+        SB_CUDA_CHECK(rb.sync());
         FA = (int)runs[0];
         FB = (int)runs[1];
     }
+    b->K = (int)K;
+    st.intersecting_pairs = K;
     {
         // synchronised past the leaf orders (when there were pairs to group; else at the end)
         const sb_status r = K > 0 ? rankResults() : SB_OK;
