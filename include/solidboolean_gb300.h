@@ -117,11 +117,13 @@ sb_status sb_result_vertices(sb_boolean *b, double *xyz, size_t cap, size_t *cou
 /* Device results: pointers stay valid until the next combine or destroy; counts are host values. */
 sb_status sb_fetch_device(sb_boolean *b, sb_op op, const uint32_t **d_tris, size_t *count);
 sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t *count);
-/* Stage dumps for parity checks (host copies). Names: "candidates" (uint32 pairs, sorted),
+/* Stage dumps for parity checks (host copies). Names: "candidates" (uint32 pairs, in emission order),
  * "intersection_pairs" (uint32 pairs), "intersection_segments" (6 doubles per intersecting pair),
  * "arrangement" (uint32 triangles), "labels" (int8 per arrangement triangle: 0 outside, 1 inside, -1 in no
- * group), "tri_mesh" (int8 per arrangement triangle: 0 first mesh, 1 second). *bytes receives the size;
- * out may be NULL. */
+ * group), "tri_mesh" (int8 per arrangement triangle: 0 first mesh, 1 second), "new_sources" (int32 per
+ * appended result vertex: 2 x its intersecting pair + the end of that pair's segment it was built from),
+ * "rank_first" / "rank_second" (int32 per triangle: position in the reference tree's leaf order). *bytes
+ * receives the size; out may be NULL. */
 sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
 void sb_boolean_destroy(sb_boolean *b);
 

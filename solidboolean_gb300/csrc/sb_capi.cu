@@ -1694,6 +1694,10 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
     } else if (n == "tri_mesh") {
         sz = (size_t)b->nTri;
         src = b->d_triMesh;
+    } else if (n == "new_sources") {
+        // per appended vertex: 2 x (its intersecting pair) + (which end of that pair's segment)
+        sz = sizeof(int) * (b->nNewV - (size_t)b->newBase);
+        src = b->d_newSrc;
     } else if (n == "rank_first" || n == "rank_second") {
         const MeshDev &M = n == "rank_first" ? b->first->d : b->second->d;
         sz = M.rankValid ? sizeof(int) * (size_t)M.nt : 0;

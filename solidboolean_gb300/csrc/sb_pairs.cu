@@ -4,7 +4,8 @@
 // src/solidboolean.cpp:94-101) emits exactly the pairs whose triangle AABBs overlap under closed intervals;
 // here one thread per first-mesh triangle (taken in Morton order, so neighbouring threads query
 // neighbouring boxes) walks the second mesh's LBVH with a private stack and writes hits through
-// warp-aggregated atomics. The set is the same; it is sorted afterwards so runs are deterministic.
+// warp-aggregated atomics. The set is the same; its order is not used (every later ordering is by unique
+// keys), so runs are deterministic without sorting it.
 //
 // Narrow phase: Guigue-Devillers (thirdparty/GuigueDevillers03/tri_tri_intersect.c:285-472) one thread per
 // candidate. Every orientation sign the reference tests is first evaluated in FP32 from rounded copies of
