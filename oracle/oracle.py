@@ -3,6 +3,8 @@
   port()       -> our C++ restatement of the reference path (oracle/sb_oracle.cpp), built by `make port`
   reference()  -> the reference's own sources compiled here (oracle/_ref/libsbref.so), built by `make ref`;
                   only available where the reference sources exist (None elsewhere)
+  obj_reference() -> the reference test driver's OBJ loader (oracle/_ref/libobjref.so, `make objref`), a
+                  function path -> (vertices, triangles); None where the reference sources are absent
 
 Both return a Checker whose run() gives a dict of numpy arrays named as in oracle/sb_oracle.h.
 """
@@ -108,3 +110,27 @@ def reference() -> Checker | None:
         build("ref")
         _cache["ref"] = Checker(REF_SO)
     return _cache["ref"]
+
+
+def obj_reference():
+    if "objref" not in _cache:
+        if not os.path.isfile(os.path.join(REF_ROOT, "test", "tiny_obj_loader.h")):
+            return None
+        build("objref")
+        L = ctypes.CDLL(os.path.join(HERE, "_ref", "libobjref.so"))
+        L.sbo_obj_load.restype = ctypes.c_int
+        L.sbo_obj_load.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p, ctypes.c_long,
+                                   ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
+
+        def load(path: str):
+            nv, nt = ctypes.c_long(), ctypes.c_long()
+            if L.sbo_obj_load(path.encode(), None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nt)) != 0:
+                raise RuntimeError(f"tinyobj could not read {path}")
+            v = np.zeros((nv.value, 3), dtype=np.float64)
+            t = np.zeros((nt.value, 3), dtype=np.uint32)
+            L.sbo_obj_load(path.encode(), v.ctypes.data, nv.value, t.ctypes.data, nt.value, ctypes.byref(nv),
+                           ctypes.byref(nt))
+            return v, t
+
+        _cache["objref"] = load
+    return _cache["objref"]

@@ -51,3 +51,18 @@ def test_obj_round_trip(tmp_path):
     v2, f2 = objio.load_obj(path)
     assert np.array_equal(f2, f.astype(np.uint32))
     assert np.allclose(v2, v, atol=1e-6)
+
+
+def test_reader_matches_reference_loader():
+    """objio against the reference test driver's own loader (tinyobjloader compiled from the reference's
+    header): identical vertices and triangles on every test mesh."""
+    load = oracle.obj_reference()
+    cases = list(_cases())
+    if load is None or not cases:
+        pytest.skip("reference sources not present")
+    for name, a, b in cases:
+        for path in (a, b):
+            v_ref, t_ref = load(path)
+            v, t = objio.load_obj(path)
+            assert np.array_equal(v, v_ref), (name, path)
+            assert np.array_equal(t, t_ref), (name, path)
