@@ -66,3 +66,34 @@ def test_reader_matches_reference_loader():
             v, t = objio.load_obj(path)
             assert np.array_equal(v, v_ref), (name, path)
             assert np.array_equal(t, t_ref), (name, path)
+
+
+def test_reader_matches_reference_loader_on_polygons(tmp_path):
+    """Faces of 4 to 9 corners, convex and concave (random star-shaped polygons in random planes), written
+    as OBJ and read by both loaders: same triangles, same vertices."""
+    load = oracle.obj_reference()
+    if load is None:
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(11)
+    lines, nv = [], 0
+    for _ in range(300):
+        k = int(rng.integers(4, 10))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, k))
+        rad = rng.uniform(0.3, 1.0, k)
+        pts2 = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1)
+        basis = np.linalg.qr(rng.standard_normal((3, 3)))[0]
+        pts = pts2 @ basis[:2] + rng.uniform(-5, 5, 3)
+        for p in pts:
+            lines.append(f"v {p[0]:.6f} {p[1]:.6f} {p[2]:.6f}")
+        order = list(range(nv + 1, nv + k + 1))
+        if rng.random() < 0.5:
+            order = order[::-1]
+        lines.append("f " + " ".join(str(i) for i in order))
+        nv += k
+    path = str(tmp_path / "polys.obj")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    v_ref, t_ref = load(path)
+    v, t = objio.load_obj(path)
+    assert np.array_equal(v, v_ref)
+    assert np.array_equal(t, t_ref)
