@@ -15,8 +15,15 @@ ARRAYS = ["cand", "isect", "seg", "newv", "newt", "groups_a_off", "groups_a", "g
           "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"]
 
 
+def _eq(x, y) -> bool:
+    x, y = np.asarray(x), np.asarray(y)
+    if x.dtype.kind == "f" or y.dtype.kind == "f":
+        return np.array_equal(x, y, equal_nan=True)  # degenerate constructions give NaN in both
+    return np.array_equal(x, y)
+
+
 def _same(a: dict, b: dict, keys=ARRAYS):
-    bad = [k for k in keys if not np.array_equal(np.asarray(a[k]), np.asarray(b[k]))]
+    bad = [k for k in keys if not _eq(a[k], b[k])]
     if int(a["status"]) != int(b["status"]):
         bad.append("status")
     return bad
@@ -49,6 +56,18 @@ def _workloads():
     for i in range(12):
         va, fa, vb, fb, _ = mg.batch_pair(rng, 4)
         yield f"batch_{i}", (va, fa, vb, fb)
+    # edge inputs: no candidates (apart, nested), every pair coplanar (identical meshes: combine fails),
+    # a lone crossing triangle pair (open loop: combine fails), an empty second mesh, touching spheres
+    v2, f2 = mg.icosphere(2)
+    f2 = np.ascontiguousarray(f2, dtype=np.uint32)
+    yield "edge_disjoint", (v2, f2, mg.transform(v2, 0.5, None, (5.0, 0.0, 0.0)), f2)
+    yield "edge_nested", (v2, f2, mg.transform(v2, 0.5, None, (0.1, 0.0, 0.0)), f2)
+    yield "edge_identical", (v2, f2, v2.copy(), f2.copy())
+    tri = np.array([[0, 1, 2]], dtype=np.uint32)
+    yield "edge_single", (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float), tri,
+                          np.array([[0.2, 0.2, -1], [0.2, 0.2, 1], [1, 1, 0.5]], float), tri)
+    yield "edge_empty_second", (v2, f2, np.zeros((0, 3)), np.zeros((0, 3), dtype=np.uint32))
+    yield "edge_touching", (v2, f2, mg.transform(v2, 1.0, None, (2.0, 0.0, 0.0)), f2)
 
 
 @pytest.mark.parametrize("name,meshes", list(_workloads()))
