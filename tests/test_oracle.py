@@ -140,3 +140,36 @@ def test_tritri_known_cases(port, case):
         assert r == 0
     if case == 2:
         assert cop == 1
+
+
+def _cube():
+    v = np.array([[x, y, z] for x in (-1, 1) for y in (-1, 1) for z in (-1, 1)], float)
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    f = []
+    for a, b, c, d in quads:
+        f += [(a, b, c), (a, c, d)]
+    return v, np.array(f, dtype=np.uint32)
+
+
+def test_port_matches_reference_on_cubes(port):
+    """Flat-faced inputs (a cube, two triangles per face, against a cube or an icosphere, random scales,
+    rotations and offsets): most of these make the reference fail (its loop building on two-triangle faces),
+    and the restatement must fail at the same stage with the same arrays, or succeed identically."""
+    ref = oracle.reference()
+    if ref is None:
+        pytest.skip("reference sources not present")
+    rng = mg.SplitMix64(3)
+    failures = 0
+    for i in range(60):
+        va, fa = _cube()
+        vb, fb = (_cube() if i % 3 == 0 else mg.icosphere(2 if i % 3 == 1 else 1))
+        va = np.ascontiguousarray(mg.transform(va, rng.uniform(0.5, 1.5), mg.rotation_matrix(rng.unit_quaternion())))
+        vb = np.ascontiguousarray(mg.transform(vb, rng.uniform(0.5, 1.5), mg.rotation_matrix(rng.unit_quaternion()),
+                                               tuple(rng.unit_vector() * rng.uniform(0.2, 1.5))))
+        fb = np.ascontiguousarray(fb, dtype=np.uint32)
+        for quantum in (100000, 100000000):
+            a = ref.run(va, fa, vb, fb, quantum)
+            b = port.run(va, fa, vb, fb, quantum)
+            assert _same(a, b) == [], (i, quantum)
+            failures += int(a["status"]) == 0
+    assert 0 < failures < 120  # both outcomes are exercised
