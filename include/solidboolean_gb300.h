@@ -128,19 +128,23 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
 void sb_boolean_destroy(sb_boolean *b);
 
 /* No counterpart in the reference. Re-triangulates cut faces exactly as sb_combine does, for callers that
- * cannot allocate device memory: code running while a CUDA graph is captured, code inside a framework that
- * owns all device memory through its own pool, real-time loops where a cudaMalloc could stall. It calls no
- * cudaMalloc/cudaFree and no allocating library routine; its workspace is a 64 MiB static device array
- * inside the library (held by every GPU that loads the library until exit). Calls whose faces need more
- * return SB_ERR_CAPACITY before launching anything.
+ * cannot allocate device memory: code inside a framework that owns all device memory through its own pool
+ * (an allocation behind its back breaks its accounting and can fail once the pool holds the free memory),
+ * and real-time loops where a cudaMalloc or cudaFree could stall. It calls no cudaMalloc/cudaFree and no
+ * allocating library routine; its workspace is a 64 MiB static device array inside the library (held by
+ * every GPU that loads the library until exit). A request whose fixed layout does not fit returns
+ * SB_ERR_CAPACITY before launching anything; one whose per-face workspace does not fit returns
+ * SB_ERR_CAPACITY after a sizing pass that writes into the shared array (the call reads that size back and
+ * synchronises its stream), without re-triangulating.
  *   d_corners   [n_faces*9]      three corners (xyz) of each face, in the face's vertex order
  *   d_seg_begin [n_faces+1]      CSR offsets of each face's segments (0 .. n_segments)
  *   d_segments  [n_segments*6]   cut segments (source xyz, target xyz) in the face's processing order
  *   d_tris      [n_faces*tri_cap*3] output: per face, local ids (0..2 corners, 3+k the face's k-th point)
  *   d_tri_count, d_point_count, d_status [n_faces] outputs (status 0 ok, 1 attach, 2 link, 3 capacity)
  *   d_points    [2*n_segments*3] output: the face's welded points at offset 2*seg_begin[f]
- * The first call on a device looks up the array's address and caches it: make it before any stream
- * capture. All calls share the array, so calls that overlap on the GPU race; serialise them. */
+ * The first call on a device (with that device current) looks up the array's address and caches it: make
+ * it before any stream capture. cudaDeviceReset invalidates the cached address. All calls share the array,
+ * so calls that overlap on the GPU race; serialise them. */
 sb_status sb_retriangulate_faces_noalloc(const double *d_corners, const int *d_seg_begin, const double *d_segments,
                                          int n_faces, int n_segments, int64_t weld_factor, int *d_tris, int tri_cap,
                                          int *d_tri_count, double *d_points, int *d_point_count, int *d_status,

@@ -19,7 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libsb_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsbref.so")
-REF_ROOT = os.environ.get("SB_REFERENCE_ROOT", "/root/reference")
+# the reference sources: $SB_REFERENCE_ROOT, else a checkout named "reference" beside this repository
+REF_ROOT = os.environ.get("SB_REFERENCE_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 _NAMES_I64 = ["status", "cand", "isect", "newt", "groups_a_off", "groups_a", "groups_b_off", "groups_b",
               "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"]

@@ -1,18 +1,28 @@
 // Allocation-free re-triangulation of cut faces.
 //
-// Some callers cannot allocate device memory: code that runs while a CUDA graph is being captured, code
-// inside a framework that owns every device allocation through its own memory pool, or a real-time loop
-// where a cudaMalloc could stall. For them sb_retriangulate_faces_noalloc runs the same per-face kernel as
+// Some callers cannot allocate device memory: code inside a framework that owns every device allocation
+// through its own memory pool (a cudaMalloc behind its back breaks its accounting and can fail once the
+// pool has taken the free memory), and real-time loops where a cudaMalloc or cudaFree could stall or
+// synchronise the device. For them sb_retriangulate_faces_noalloc runs the same per-face kernel as
 // sb_combine (k_faces, sb_faces.cu) with its per-face workspace taken from one file-scope static device
 // array of fixed size instead of from a cudaMalloc'd buffer. The caller passes every input and output.
 //
 // Rules of use:
 //   * the workspace is kNoAllocScratchBytes (64 MiB) per device; every GPU that loads the library holds it
-//     until the process exits; a call whose faces need more returns SB_ERR_CAPACITY before any launch;
-//   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) and caches it:
-//     make that first call before any stream capture;
-//   * all calls share the array and it keeps the previous call's contents: calls that can overlap on the
-//     GPU (different streams, or threads) race and must be serialised by the caller;
+//     until the process exits;
+//   * size checks: a request whose fixed layout (per-face tables, per-segment keys) does not fit returns
+//     SB_ERR_CAPACITY before any launch; the per-face workspace total is only known after a sizing pass
+//     that runs on the GPU and writes into the shared array, so a request that fails that second check
+//     returns SB_ERR_CAPACITY after the sizing pass, without running the re-triangulation;
+//   * the call reads that total back and waits for its stream (cudaStreamSynchronize) before it launches
+//     the re-triangulation;
+//   * the first call on a device, with that device current, looks up the array's device address
+//     (cudaGetSymbolAddress) and caches it per device: make that first call before any stream capture.
+//     cudaDeviceReset, or anything else that destroys the primary context, invalidates the cached
+//     address: do not call this entry point again in a process after that;
+//   * all calls share the array and it keeps the previous call's contents (the parts that must start at
+//     zero are cleared by each call): calls that can overlap on the GPU (different streams, or threads)
+//     race and must be serialised by the caller;
 //   * no cudaMalloc, cudaFree or allocating library routine is called (the prefix sum uses CUB with its
 //     temporary storage carved from the same array).
 #include <algorithm>

@@ -1,7 +1,8 @@
 """The allocation-free face re-triangulation entry point against the regular path.
 
-sb_retriangulate_faces_noalloc serves callers that cannot allocate device memory (graph capture, a
-framework's own memory pool, real-time loops): its workspace is a static device array in the library.
+sb_retriangulate_faces_noalloc serves callers that cannot allocate device memory (a framework that owns all
+device memory through its own pool, real-time loops where an allocation could stall): its workspace is a
+static device array in the library.
 This test feeds it the cut faces of a boolean computed by the regular entry points (sb_combine), twice in
 a row, and checks that both calls return the same triangles, and that those triangles, mapped to result
 vertex ids, are exactly the re-triangulated part of the regular arrangement. The file sorts last so that a
@@ -68,7 +69,7 @@ def test_noalloc_matches_combine_twice(gpu_lib):
     d_corners = torch.from_numpy(np.ascontiguousarray(corners)).to(dev)
     d_begin = torch.from_numpy(begin).to(dev)
     d_segs = torch.from_numpy(np.ascontiguousarray(segs)).to(dev)
-    outs = []
+    outs, frees = [], []
     for _ in range(2):
         d_tris = torch.full((nf * cap * 3,), -7, dtype=torch.int32, device=dev)
         d_tc = torch.zeros(nf, dtype=torch.int32, device=dev)
@@ -76,13 +77,18 @@ def test_noalloc_matches_combine_twice(gpu_lib):
         d_pc = torch.zeros(nf, dtype=torch.int32, device=dev)
         d_st = torch.full((nf,), -1, dtype=torch.int32, device=dev)
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(dev)[0]
         r = fn(d_corners.data_ptr(), d_begin.data_ptr(), d_segs.data_ptr(), nf, ns, WELD, d_tris.data_ptr(), cap,
                d_tc.data_ptr(), d_pts.data_ptr(), d_pc.data_ptr(), d_st.data_ptr(), None)
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(dev)[0]
         assert r == sbg.SB_OK, L.sb_last_error()
+        frees.append((free_before, free_after))
         outs.append([t.cpu().numpy() for t in (d_tris, d_tc, d_pts, d_pc, d_st)])
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+    # the second call (its kernels already loaded by the first) leaves the device's free memory unchanged
+    assert frees[1][0] == frees[1][1], frees
     tris, tc, pts, pc, st = outs[0]
     assert (st == 0).all()
 
