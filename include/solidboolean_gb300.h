@@ -80,6 +80,9 @@ typedef struct sb_stats {
     uint32_t loop_vertices;      /* vertices of the cut loops */
     uint32_t loop_bad_degree;    /* loop vertices whose degree is not 2 */
     uint32_t duplicate_halfedges;
+    uint32_t loops;              /* cut loops of the first mesh */
+    uint32_t order_fallbacks;    /* cut faces whose place in the reference's processing order could not be
+                                    derived (they keep triangle-index order; 0 when the order is exact) */
     double stage_ms[8];          /* broad, narrow, faces, weld, assemble, groups, sides, fetch (device time) */
 } sb_stats;
 

@@ -23,7 +23,8 @@ REF_SO = os.path.join(HERE, "_ref", "libsbref.so")
 REF_ROOT = os.environ.get("SB_REFERENCE_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 _NAMES_I64 = ["status", "cand", "isect", "newt", "groups_a_off", "groups_a", "groups_b_off", "groups_b",
-              "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"]
+              "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b", "ctx_a", "ctx_b",
+              "loops_a_off", "loops_a", "tri_ranges"]
 _NAMES_F64 = ["seg", "newv", "time_ms"]
 _SHAPES = {"cand": (-1, 2), "seg": (-1, 6), "newv": (-1, 3), "newt": (-1, 3), "union": (-1, 3),
            "diff": (-1, 3), "intersect": (-1, 3)}

@@ -779,6 +779,10 @@ struct Boolean {
     std::vector<bool> sidesA, sidesB;
     std::unordered_set<size_t> cutA, cutB;
     double tm[7] = {0, 0, 0, 0, 0, 0, 0};
+    // debug views of intermediate orders: cut faces in the contexts' iteration order, the first mesh's loops
+    std::vector<size_t> ctxOrderA, ctxOrderB;
+    std::vector<std::vector<size_t>> loopsFirst;
+    int64_t triRanges[4] = {0, 0, 0, 0}; // uncut first, uncut second, re-triangulated first, second
 
     size_t addNewPoint(const V3 &p)
     {
@@ -1044,6 +1048,10 @@ struct Boolean {
             ctxB[pr.second].segment(S, T);
         }
         auto t2 = C::now();
+        for (const auto &it : ctxA)
+            ctxOrderA.push_back(it.first);
+        for (const auto &it : ctxB)
+            ctxOrderB.push_back(it.first);
         std::unordered_map<size_t, std::unordered_set<size_t>> edgesA, edgesB;
         std::vector<std::vector<size_t>> loopsA;
         std::unordered_map<uint64_t, size_t> heA, heB;
@@ -1057,13 +1065,20 @@ struct Boolean {
         tm[0] = ms(t0, t1);
         tm[1] = ms(t1, t2);
         tm[2] = ms(t2, t3);
+        triRanges[0] = (int64_t)remA;
+        triRanges[1] = (int64_t)remB;
+        const size_t retri0 = newT.size();
         if (!retri(ctxA, A, 0, edgesA, heA))
             return false;
+        triRanges[2] = (int64_t)(newT.size() - retri0);
         if (!retri(ctxB, B, A->v.size(), edgesB, heB))
             return false;
+        triRanges[3] = (int64_t)(newT.size() - retri0) - triRanges[2];
         auto t4 = C::now();
         tm[3] = ms(t3, t4);
-        if (!loops(edgesA, loopsA))
+        const bool loopsOk = loops(edgesA, loopsA);
+        loopsFirst = loopsA;
+        if (!loopsOk)
             return false;
         auto t5 = C::now();
         tm[4] = ms(t4, t5);
@@ -1176,6 +1191,12 @@ extern "C" void *sbo_run(const double *va, size_t nva, const uint32_t *ta, size_
     };
     groups(sb.groupsA, "groups_a_off", "groups_a");
     groups(sb.groupsB, "groups_b_off", "groups_b");
+    groups(sb.loopsFirst, "loops_a_off", "loops_a");
+    d->i64["tri_ranges"] = {sb.triRanges[0], sb.triRanges[1], sb.triRanges[2], sb.triRanges[3]};
+    for (size_t f : sb.ctxOrderA)
+        d->i64["ctx_a"].push_back((int64_t)f);
+    for (size_t f : sb.ctxOrderB)
+        d->i64["ctx_b"].push_back((int64_t)f);
     d->i64["sides_a"];
     d->i64["sides_b"];
     for (bool s : sb.sidesA)

@@ -14,6 +14,10 @@
  *   sides_a, sides_b  group sides (1 = inside the other mesh)
  *   union, diff, intersect  [n*3] the three fetch results
  *   leaforder_a/_b    triangles in leaf order of each mesh's AABB tree
+ *   ctx_a, ctx_b      (restatement only) cut faces of each mesh in their context map's iteration order
+ *   loops_a_off/_a    (restatement only) CSR of the first mesh's cut loops, as buildPolygonsFromEdges lists them
+ *   tri_ranges        (restatement only) [4] arrangement triangles: uncut first, uncut second, re-triangulated
+ *                     first, re-triangulated second
  *   time_ms           per-stage wall times (prepareA, prepareB, search, process, addUnint, retri, loops,
  *                     groups, sides)
  */

@@ -49,7 +49,8 @@ class Stats(ctypes.Structure):
                 ("box_fallbacks", ctypes.c_uint64), ("regions_first", ctypes.c_uint32),
                 ("regions_second", ctypes.c_uint32), ("failed_faces", ctypes.c_uint32),
                 ("loop_vertices", ctypes.c_uint32), ("loop_bad_degree", ctypes.c_uint32),
-                ("duplicate_halfedges", ctypes.c_uint32), ("stage_ms", ctypes.c_double * 8)]
+                ("duplicate_halfedges", ctypes.c_uint32), ("loops", ctypes.c_uint32),
+                ("order_fallbacks", ctypes.c_uint32), ("stage_ms", ctypes.c_double * 8)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsolidboolean_gb300.so")
-SOURCES = ["sb_prepare.cu", "sb_refrank.cu", "sb_pairs.cu", "sb_faces.cu", "sb_assemble.cu", "sb_capi.cu",
+SOURCES = ["sb_prepare.cu", "sb_refrank.cu", "sb_pairs.cu", "sb_faces.cu", "sb_assemble.cu", "sb_order.cu", "sb_capi.cu",
            "sb_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",

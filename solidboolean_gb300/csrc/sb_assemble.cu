@@ -22,12 +22,13 @@
 
 namespace sbg {
 
-// ---- global weld ------------------------------------------------------------------------------------
-// seq = position of a cut point in (face order, local order); slots claim by the first seq to arrive and
-// keep the minimum seq of the key
-__global__ void k_weld_insert(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ faceNpts,
-                              const Key *__restrict__ keys, int *slotOwner, int *slotMin, uint32_t mask,
-                              int *pointSlot)
+// ---- global weld ----------------------------------------------------------------------------------
+// A cut point's place in the reference's sequence is ptRef[f] + k: faces in their processing order (the
+// first mesh's, then the second's), points in each face's local order. Slots are claimed by the first
+// storage position to arrive (for the key comparison) and keep the smallest sequence position of the key.
+__global__ void k_weld_insert(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ ptRef,
+                              const int *__restrict__ faceNpts, const Key *__restrict__ keys, int *slotOwner,
+                              int *slotMin, uint32_t mask, int *pointSlot)
 {
     int f = blockIdx.x;
     if (f >= nFaces)
@@ -40,7 +41,7 @@ __global__ void k_weld_insert(int nFaces, const int *__restrict__ ptOff, const i
         for (uint32_t probe = 0; probe <= mask; ++probe) {
             int o = atomicCAS(slotOwner + s, -1, seq);
             if (o == -1 || key_eq(keys[o], key)) {
-                atomicMin(slotMin + s, seq);
+                atomicMin(slotMin + s, ptRef[f] + k);
                 pointSlot[seq] = (int)s;
                 break;
             }
@@ -49,35 +50,46 @@ __global__ void k_weld_insert(int nFaces, const int *__restrict__ ptOff, const i
     }
 }
 
-// first occurrences flagged per seq position
-__global__ void k_weld_first(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ faceNpts,
-                             const int *__restrict__ pointSlot, const int *__restrict__ slotMin, int *isFirst)
+// first occurrences flagged at their sequence positions (capacity slots past a face's points stay 0)
+__global__ void k_weld_first(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ ptRef,
+                             const int *__restrict__ faceNpts, const int *__restrict__ pointSlot,
+                             const int *__restrict__ slotMin, int *isFirst)
 {
     int f = blockIdx.x;
     if (f >= nFaces)
         return;
     int n = faceNpts[f];
     for (int k = threadIdx.x; k < ptOff[f + 1] - ptOff[f]; k += blockDim.x) {
-        int seq = ptOff[f] + k;
-        isFirst[seq] = (k < n && slotMin[pointSlot[seq]] == seq) ? 1 : 0;
+        const int rs = ptRef[f] + k;
+        isFirst[rs] = (k < n && slotMin[pointSlot[ptOff[f] + k]] == rs) ? 1 : 0;
     }
 }
 
-__global__ void k_weld_number(int nSeq, const int *__restrict__ isFirst, const int *__restrict__ firstRank,
-                              const int *__restrict__ pointSlot, int *slotRank, const d3 *__restrict__ pts,
-                              double *newV, int vbase, const int *__restrict__ ptSrc, int *newSrc)
+// appended vertex r = rank of its first occurrence in the sequence (addNewPoint numbering), with the
+// coordinates of that occurrence
+__global__ void k_weld_number(int nFaces, const int *__restrict__ ptOff, const int *__restrict__ ptRef,
+                              const int *__restrict__ faceNpts, const int *__restrict__ isFirst,
+                              const int *__restrict__ firstRank, const int *__restrict__ pointSlot, int *slotRank,
+                              const d3 *__restrict__ pts, double *newV, int vbase, const int *__restrict__ ptSrc,
+                              int *newSrc)
 {
-    int seq = blockIdx.x * blockDim.x + threadIdx.x;
-    if (seq >= nSeq || !isFirst[seq])
+    int f = blockIdx.x;
+    if (f >= nFaces)
         return;
-    int r = firstRank[seq];
-    slotRank[pointSlot[seq]] = r;
-    newSrc[r] = ptSrc[seq];
-    d3 p = pts[seq];
-    double *o = newV + 3 * (size_t)(vbase + r);
-    o[0] = p.x;
-    o[1] = p.y;
-    o[2] = p.z;
+    int n = faceNpts[f];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int rs = ptRef[f] + k, seq = ptOff[f] + k;
+        if (!isFirst[rs])
+            continue;
+        const int r = firstRank[rs];
+        slotRank[pointSlot[seq]] = r;
+        newSrc[r] = ptSrc[seq];
+        const d3 p = pts[seq];
+        double *o = newV + 3 * (size_t)(vbase + r);
+        o[0] = p.x;
+        o[1] = p.y;
+        o[2] = p.z;
+    }
 }
 
 // ---- arrangement ------------------------------------------------------------------------------------
@@ -140,11 +152,15 @@ __global__ void k_retri(int nFaces, const int *__restrict__ faceSide, const int 
 }
 
 // ---- cut loops (first mesh's cut edges) ----------------------------------------------------------------
+// Directed entry e of first-mesh face f, (u -> v), is the reference's `edges[u].insert(v); edges[v].insert(u)`
+// at sequence slots 2 (edgeRef[f] + e) and that + 1 (src/solidboolean.cpp:397-404): u becomes a key of the
+// loop map at the first slot, v at the second, v joins u's set at the first, u joins v's set at the second.
+// Per undirected edge (lo, hi) of the table: slotLo = when hi joined lo's set, slotHi = when lo joined hi's.
 __global__ void k_cut_edges(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ faceNedges,
-                            const int *__restrict__ edgeOff, const int *__restrict__ faceEdges,
-                            const int *__restrict__ ptOff, const int *__restrict__ pointSlot,
-                            const int *__restrict__ slotRank, uint64_t *edgeKeys, int *edgeVals, uint32_t mask,
-                            int sideWanted)
+                            const int *__restrict__ edgeOff, const int *__restrict__ edgeRef,
+                            const int *__restrict__ faceEdges, const int *__restrict__ ptOff,
+                            const int *__restrict__ pointSlot, const int *__restrict__ slotRank, uint64_t *edgeKeys,
+                            int *edgeVals, uint32_t mask, int *slotLo, int *slotHi, int *firstOcc, int sideWanted)
 {
     int f = blockIdx.x;
     if (f >= nFaces || faceSide[f] != sideWanted)
@@ -155,12 +171,22 @@ __global__ void k_cut_edges(int nFaces, const int *__restrict__ faceSide, const 
         uint32_t v = (uint32_t)slotRank[pointSlot[ptOff[f] + e[1] - 3]];
         if (u == v)
             continue;
+        const int slot = 2 * (edgeRef[f] + k);
         uint32_t lo = min(u, v), hi = max(u, v);
-        u64map_insert_min(edgeKeys, edgeVals, mask, ((uint64_t)lo << 32) | hi, 0);
+        const int s = u64map_insert_min_slot(edgeKeys, edgeVals, mask, ((uint64_t)lo << 32) | hi, 0);
+        if (s >= 0) {
+            atomicMin(slotLo + s, u == lo ? slot : slot + 1);
+            atomicMin(slotHi + s, u == lo ? slot + 1 : slot);
+        }
+        atomicMin(firstOcc + u, slot);
+        atomicMin(firstOcc + v, slot + 1);
     }
 }
 
-__global__ void k_loop_degree(uint32_t cap, const uint64_t *__restrict__ edgeKeys, int *degree)
+// neighbour count of every loop vertex, and its first two neighbours with the slot at which each joined
+// its set
+__global__ void k_loop_degree(uint32_t cap, const uint64_t *__restrict__ edgeKeys, const int *__restrict__ slotLo,
+                              const int *__restrict__ slotHi, int *degree, int *nbr, int *nbrSlot)
 {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cap)
@@ -168,8 +194,17 @@ __global__ void k_loop_degree(uint32_t cap, const uint64_t *__restrict__ edgeKey
     uint64_t k = edgeKeys[s];
     if (k == kEmpty64)
         return;
-    atomicAdd(degree + (uint32_t)(k >> 32), 1);
-    atomicAdd(degree + (uint32_t)(k & 0xFFFFFFFFu), 1);
+    const int lo = (int)(k >> 32), hi = (int)(k & 0xFFFFFFFFu);
+    const int a = atomicAdd(degree + lo, 1);
+    if (a < 2) {
+        nbr[2 * lo + a] = hi;
+        nbrSlot[2 * lo + a] = slotLo[s];
+    }
+    const int b = atomicAdd(degree + hi, 1);
+    if (b < 2) {
+        nbr[2 * hi + b] = lo;
+        nbrSlot[2 * hi + b] = slotHi[s];
+    }
 }
 
 __global__ void k_loop_check(int n, const int *__restrict__ degree, unsigned int *counters)
@@ -201,16 +236,6 @@ __global__ void k_halfedges(int nTri, const uint32_t *__restrict__ newT, const i
     const int lastEdge = t < uncutAll ? truncOcc[m] - 3 * origUncut[t] : 2;
     for (int i = 0; i < 3 && i <= lastEdge; ++i)
         u64map_insert_min(keys, vals, mask, he_key(v[i], v[(i + 1) % 3]), t);
-}
-
-__device__ __forceinline__ bool is_cut_edge(const uint64_t *edgeKeys, const int *edgeVals, uint32_t emask, uint32_t u,
-                                            uint32_t v, uint32_t newBase)
-{
-    if (u < newBase || v < newBase)
-        return false;
-    uint32_t a = u - newBase, b = v - newBase;
-    uint32_t lo = min(a, b), hi = max(a, b);
-    return u64map_find(edgeKeys, edgeVals, emask, ((uint64_t)lo << 32) | hi) >= 0;
 }
 
 __device__ int uf_find(int *parent, int x)
@@ -390,18 +415,24 @@ __global__ void k_region_rep(int nTri, const int *__restrict__ root, const int *
     }
 }
 
+// Regions without seeds are the reference's remaining groups (src/solidboolean.cpp:231-238): each is flooded
+// from its smallest uncut triangle, whose side is queried; regions with seeds take their groups' sides.
 __global__ void k_region_list(int nTri, const int *__restrict__ root, const int *__restrict__ seedMin,
-                              const int *__restrict__ remMin, int *repOfRoot, int *reps, unsigned int *nReps,
+                              const int *__restrict__ remMin, int *regionQuery, int *qTri, unsigned int *nQueries,
                               const int8_t *__restrict__ triMesh, unsigned int *regionsPerMesh)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nTri || root[t] != t)
         return;
-    int rep = seedMin[t] != INT_MAX ? seedMin[t] : (remMin[t] != INT_MAX ? remMin[t] : -1);
-    repOfRoot[t] = rep;
-    if (rep >= 0) {
-        unsigned int k = atomicAdd(nReps, 1u);
-        reps[k] = t;
+    regionQuery[t] = -1;
+    if (seedMin[t] != INT_MAX) {
+        atomicAdd(regionsPerMesh + triMesh[t], 1u);
+        return;
+    }
+    if (remMin[t] != INT_MAX) {
+        unsigned int k = atomicAdd(nQueries, 1u);
+        qTri[k] = remMin[t];
+        regionQuery[t] = (int)k;
         atomicAdd(regionsPerMesh + triMesh[t], 1u);
     }
 }
@@ -507,15 +538,16 @@ __device__ __forceinline__ void side_record(const SideRay &ray, int rayId, const
 // against the outward-rounded query is conservative; side_hit then applies the reference's FP64 box test.
 constexpr int kBruteRays = 96;
 
-__global__ void k_side_rays(int nRays, const int *__restrict__ reps, const int *__restrict__ repOfRoot,
-                            const uint32_t *__restrict__ newT, const double *__restrict__ newV,
-                            const int8_t *__restrict__ triMesh, SideRay *rays, int *hitCount)
+// three rays per side query (a group's first triangle, or a remaining region's smallest uncut triangle)
+__global__ void k_side_rays(int nRays, const int *__restrict__ qTri, const uint32_t *__restrict__ newT,
+                            const double *__restrict__ newV, const int8_t *__restrict__ triMesh, SideRay *rays,
+                            int *hitCount)
 {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nRays)
         return;
-    const int r = reps[w / 3];
-    rays[w] = side_ray(repOfRoot[r], w % 3, r, newT, newV, triMesh);
+    const int q = w / 3;
+    rays[w] = side_ray(qTri[q], w % 3, q, newT, newV, triMesh);
     hitCount[w] = 0;
 }
 
@@ -710,21 +742,6 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
     }
 }
 
-__global__ void k_labels(int nTri, const int *__restrict__ root, const int *__restrict__ repOfRoot,
-                         const int *__restrict__ insideCount, int8_t *label)
-{
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nTri)
-        return;
-    int r = root[t];
-    if (repOfRoot[r] < 0) {
-        label[t] = -1;
-        return;
-    }
-    // (float)insideCount / 3 > 0.5
-    label[t] = ((float)insideCount[r] / 3.0f > 0.5f) ? 1 : 0;
-}
-
 // fetch flags: union keeps outside of both, intersect inside of both, diff outside of the first and
 // inside of the second (reversed) (src/solidboolean.cpp:512-565)
 // Selection of the three results (src/solidboolean.cpp:512-570): union keeps the first mesh's outside and the
@@ -799,23 +816,25 @@ void launch_weld(const AsmArgs &g, cudaStream_t s)
         return;
     {
         KTime kt("k_weld_insert", s);
-        SB_COUNT(k_weld_insert)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.cutKeys, g.weldOwner, g.weldMin,
-                                          g.weldMask, g.pointSlot);
+        SB_COUNT(k_weld_insert)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.ptRef, g.faceNpts, g.cutKeys, g.weldOwner,
+                                                        g.weldMin, g.weldMask, g.pointSlot);
     }
     {
         KTime kt("k_weld_first", s);
-        SB_COUNT(k_weld_first)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.faceNpts, g.pointSlot, g.weldMin, g.isFirst);
+        SB_COUNT(k_weld_first)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.ptRef, g.faceNpts, g.pointSlot, g.weldMin,
+                                                       g.isFirst);
     }
 }
 
 void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s)
 {
-    if (nSeq <= 0)
+    if (nSeq <= 0 || g.nFaces <= 0)
         return;
     {
         KTime kt("k_weld_number", s);
-        SB_COUNT(k_weld_number)<<<nb(nSeq, 256), 256, 0, s>>>(nSeq, g.isFirst, g.firstRank, g.pointSlot, g.slotRank, g.cutPts,
-                                                g.newV, g.newBase, g.ptSrc, g.newSrc);
+        SB_COUNT(k_weld_number)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.ptOff, g.ptRef, g.faceNpts, g.isFirst, g.firstRank,
+                                                        g.pointSlot, g.slotRank, g.cutPts, g.newV, g.newBase, g.ptSrc,
+                                                        g.newSrc);
     }
 }
 
@@ -856,12 +875,16 @@ void launch_loops(const AsmArgs &g, cudaStream_t s)
     if (g.nFaces > 0)
         {
             KTime kt("k_cut_edges", s);
-            SB_COUNT(k_cut_edges)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceNedges, g.edgeOff, g.faceEdges, g.ptOff,
-                                            g.pointSlot, g.slotRank, g.edgeKeys, g.edgeVals, g.edgeMask, 0);
+            SB_COUNT(k_cut_edges)<<<g.nFaces, 32, 0, s>>>(g.nFaces, g.faceSide, g.faceNedges, g.edgeOff, g.edgeRef,
+                                                          g.faceEdges, g.ptOff, g.pointSlot, g.slotRank, g.edgeKeys,
+                                                          g.edgeVals, g.edgeMask, g.edgeSlotLo, g.edgeSlotHi,
+                                                          g.firstOcc, 0);
         }
     {
         KTime kt("k_loop_degree", s);
-        SB_COUNT(k_loop_degree)<<<nb((size_t)g.edgeMask + 1, 256), 256, 0, s>>>(g.edgeMask + 1, g.edgeKeys, g.degree);
+        SB_COUNT(k_loop_degree)<<<nb((size_t)g.edgeMask + 1, 256), 256, 0, s>>>(g.edgeMask + 1, g.edgeKeys, g.edgeSlotLo,
+                                                                               g.edgeSlotHi, g.degree, g.nbr,
+                                                                               g.nbrSlot);
     }
     if (g.nNew > 0)
         {
@@ -911,8 +934,9 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
     }
     {
         KTime kt("k_region_list", s);
-        SB_COUNT(k_region_list)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot, g.reps,
-                                                  g.counters + kCntReps, g.triMesh, g.counters + kCntRegionsA);
+        SB_COUNT(k_region_list)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot,
+                                                                g.qTri, g.counters + kCntReps, g.triMesh,
+                                                                g.counters + kCntRegionsA);
     }
 }
 
@@ -934,17 +958,17 @@ size_t side_layout(AsmArgs &g, int nRays, char *base)
     return c.off;
 }
 
-void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s)
+void launch_sides(const AsmArgs &g, unsigned int nQueries, bool fp64, cudaStream_t s)
 {
-    const int nRays = 3 * (int)nReps;
-    if (nReps > 0) {
+    const int nRays = 3 * (int)nQueries;
+    if (nQueries > 0) {
         KTime kt("k_sides", s);
         SideRay *rays = reinterpret_cast<SideRay *>(g.sideRays);
         Key *hits = reinterpret_cast<Key *>(g.sideHits);
         int *pairCount = g.sideHitCount + nRays; // one past the per-ray counts
         cudaMemsetAsync(pairCount, 0, sizeof(int), s);
-        SB_COUNT(k_side_rays)<<<nb(nRays, 128), 128, 0, s>>>(nRays, g.reps, g.repOfRoot, g.newT, g.newV, g.triMesh,
-                                                             rays, g.sideHitCount);
+        SB_COUNT(k_side_rays)<<<nb(nRays, 128), 128, 0, s>>>(nRays, g.qTri, g.newT, g.newV, g.triMesh, rays,
+                                                             g.sideHitCount);
         if (nRays <= kBruteRays) {
             // few rays: every triangle against all of them
             for (int target = 0; target < 2; ++target) {
@@ -978,11 +1002,6 @@ void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t 
         SB_COUNT(k_side_parity)<<<nb(32 * (size_t)nRays, 128), 128, 0, s>>>(nRays, rays, hits, g.sideHitCount,
                                                                             g.insideCount);
     }
-    if (g.nTri > 0)
-        {
-            KTime kt("k_labels", s);
-            SB_COUNT(k_labels)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.repOfRoot, g.insideCount, g.label);
-        }
 }
 
 void launch_fetch_flags(const AsmArgs &g, int *flag, cudaStream_t s)

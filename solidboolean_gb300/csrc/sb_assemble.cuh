@@ -10,7 +10,7 @@ namespace sbg {
 enum {
     kCntLoopVerts = 0,   // [0] loop vertices, [1] loop vertices with degree != 2
     kCntDupHalfedge = 2, // triangles' half-edges whose table owner is another triangle
-    kCntReps = 3,        // number of regions with a representative
+    kCntReps = 3,        // number of side queries (groups' first triangles, remaining regions)
     kCntRegionsA = 4,    // [4] first mesh, [5] second mesh
     kCntSideErrors = 6,  // hit-buffer or stack overflow in the side rays
     kCntCount = 8
@@ -29,6 +29,7 @@ struct AsmArgs {
     int *weldOwner, *weldMin;
     uint32_t weldMask;
     int *pointSlot, *isFirst, *firstRank, *slotRank;
+    const int *ptRef;   // per face: its points' first position in the reference's sequence (processing order)
     int newBase; // = A.nv + B.nv
     const int *ptSrc; // per cut point: 2 x (intersecting pair) + segment end (see FaceArgs::ptSrc)
     int *newSrc;      // per appended vertex: the source of the point that represents its weld class
@@ -46,11 +47,17 @@ struct AsmArgs {
     int *edgeVals;
     uint32_t edgeMask;
     int *degree;
+    const int *edgeRef;          // per face: its directed cut edges' first position in the processing order
+    int *edgeSlotLo, *edgeSlotHi; // per edge-table slot: when each end joined the other's neighbour set
+    int *firstOcc;               // per appended vertex: its first slot in the loop map's insertion sequence
+    int *nbr, *nbrSlot;          // per appended vertex: two neighbours on the loops and their joining slots
     // groups
     uint64_t *heKeysA, *heKeysB;
     int *heValsA, *heValsB;
     uint32_t heMask;
-    int *parent, *seedFlag, *seedMin, *remMin, *repOfRoot, *reps, *insideCount;
+    // repOfRoot: per region root, its side query (-1: none); qTri: each side query's triangle; insideCount: per
+    // query, the rays (of three) that found the point inside
+    int *parent, *seedFlag, *seedMin, *remMin, *repOfRoot, *qTri, *insideCount;
     // grouping through the input meshes' edge adjacency (both meshes hold every directed edge once): the
     // per-mesh half-edge tables then hold the re-triangulated triangles only
     int useAdj;
@@ -68,13 +75,73 @@ struct AsmArgs {
     int sidePairCap;
 };
 
+#ifdef __CUDACC__
+// (u, v) lies on a cut loop: both are appended vertices and the first mesh's cut edges hold the pair
+__device__ __forceinline__ bool is_cut_edge(const uint64_t *edgeKeys, const int *edgeVals, uint32_t emask, uint32_t u,
+                                            uint32_t v, uint32_t newBase)
+{
+    if (u < newBase || v < newBase)
+        return false;
+    uint32_t a = u - newBase, b = v - newBase;
+    uint32_t lo = min(a, b), hi = max(a, b);
+    return u64map_find(edgeKeys, edgeVals, emask, ((uint64_t)lo << 32) | hi) >= 0;
+}
+
+// The triangle the reference's flood reaches from arrangement triangle t across its edge i (v[i] -> v[i+1]),
+// or -1: the half-edge is a cut-loop edge, t is not its table owner (a repeated half-edge is crossed by its
+// first owner only), or the reverse half-edge has no owner (src/solidboolean.cpp:212-229). Through the input
+// adjacency when both meshes hold every directed edge once (the tables then hold the re-triangulated
+// triangles only), else through the full half-edge tables.
+__device__ __forceinline__ int arr_twin(const AsmArgs &g, int t, int i)
+{
+    const int retriBase = g.uncutA + g.uncutB;
+    const uint32_t *v = g.newT + 3 * (size_t)t;
+    const int side = g.triMesh[t];
+    const MeshDev &M = side == 0 ? g.A : g.B;
+    const uint64_t *keys = side == 0 ? g.heKeysA : g.heKeysB;
+    const int *vals = side == 0 ? g.heValsA : g.heValsB;
+    const uint32_t a = v[i], b = v[(i + 1) % 3];
+    const uint32_t newBase = (uint32_t)g.newBase;
+    if (g.useAdj && t < retriBase) {
+        const int *cut = side == 0 ? g.cutA : g.cutB;
+        const int *urank = side == 0 ? g.uncutRankA : g.uncutRankB;
+        const int outBase = side == 0 ? 0 : g.uncutA;
+        const int j = M.adj[3 * (size_t)g.origUncut[t] + i];
+        if (j < 0)
+            return -1;
+        return !cut[j] ? outBase + urank[j] : u64map_find(keys, vals, g.heMask, he_key(b, a));
+    }
+    const int owner = u64map_find(keys, vals, g.heMask, he_key(a, b));
+    if (is_cut_edge(g.edgeKeys, g.edgeVals, g.edgeMask, a, b, newBase) || owner != t)
+        return -1;
+    int tw = u64map_find(keys, vals, g.heMask, he_key(b, a));
+    if (g.useAdj && tw < 0 && a < newBase && b < newBase) {
+        // an original edge of the cut face: the uncut neighbour across it
+        const int *cut = side == 0 ? g.cutA : g.cutB;
+        const int *urank = side == 0 ? g.uncutRankA : g.uncutRankB;
+        const int outBase = side == 0 ? 0 : g.uncutA;
+        const uint32_t vbase = side == 0 ? 0u : (uint32_t)g.A.nv;
+        const int face = g.faceTri[g.retriFace[t - retriBase]];
+        const uint32_t *c = M.t + 3 * (size_t)face;
+        for (int kk = 0; kk < 3; ++kk)
+            if (c[kk] + vbase == a && c[(kk + 1) % 3] + vbase == b) {
+                const int j = M.adj[3 * (size_t)face + kk];
+                if (j >= 0 && !cut[j])
+                    tw = outBase + urank[j];
+                break;
+            }
+    }
+    return tw;
+}
+#endif
+
 void launch_weld(const AsmArgs &g, cudaStream_t s);
 void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s);
 void launch_mark_cut(const AsmArgs &g, cudaStream_t s);
 void launch_arrangement(const AsmArgs &g, cudaStream_t s);
 void launch_loops(const AsmArgs &g, cudaStream_t s);
 void launch_groups(const AsmArgs &g, cudaStream_t s);
-void launch_sides(const AsmArgs &g, unsigned int nReps, bool fp64, cudaStream_t s);
+void launch_sides(const AsmArgs &g, unsigned int nQueries, bool fp64, cudaStream_t s);
 // layout of the side-ray buffers for nRays rays (base null: bytes only)
 size_t side_layout(AsmArgs &g, int nRays, char *base);
 // the three results at once: flags [op * (nTri + 1) + t], one exclusive scan over all 3 (nTri + 1), writes

@@ -24,6 +24,7 @@
 #include "sb_common.cuh"
 #include "sb_faces.cuh"
 #include "sb_internal.h"
+#include "sb_order.cuh"
 #include "sb_pairs.cuh"
 
 namespace sbg {
@@ -585,7 +586,7 @@ struct sb_boolean {
     sb_options opts;
     cudaStream_t s = nullptr;
     // working and result buffers
-    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small, trunc, sides;
+    DevBuf cand, isect, faces, scratch, cut, weld, arr, groups, res, cub, small, trunc, sides, order, flood;
     unsigned int candCap = 0;
     bool combined = false;
     sb_status status = SB_ERR_NOT_COMBINED;
@@ -921,6 +922,8 @@ sb_status combine_impl(sb_boolean *b)
     int *faceNedges = (int *)(fb + o_fne), *retriRank = (int *)(fb + o_rr);
     SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
     long long totals[4] = {0, 0, 0, 0};
+    int *faceRank = nullptr, *faceByRank = nullptr, *ptRef = nullptr, *edgeRef = nullptr, *retriRef = nullptr;
+    int *rankTmp[3] = {nullptr, nullptr, nullptr}, *rankTot = nullptr;
     if (nFaces > 0) {
         SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
@@ -939,6 +942,70 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
             return cub::DeviceScan::ExclusiveSum(tmp, bytes, edgeCap, edgeOff, nFaces + 1, s);
         }));
+        // the reference's processing order of the cut faces: each face keyed by its first pair's place in the
+        // tree traversal, sorted, then ordered like the context map iterates them
+        Carve co;
+        const size_t o_fk = co.take<unsigned long long>(nFaces), o_fks = co.take<unsigned long long>(nFaces);
+        const size_t o_fv = co.take<int>(nFaces), o_fvs = co.take<int>(nFaces);
+        const size_t o_fr = co.take<int>(nFaces + 1), o_fbr = co.take<int>(nFaces + 1);
+        const size_t o_ik = co.take<uint32_t>(nFaces + 1);
+        const size_t o_hA = co.take<int>(hash_scratch_ints(FA)), o_hB = co.take<int>(hash_scratch_ints(FB));
+        const size_t o_pr = co.take<int>(nFaces + 1), o_er = co.take<int>(nFaces + 1), o_rr2 = co.take<int>(nFaces + 1);
+        const size_t o_t0 = co.take<int>(nFaces + 1), o_t1 = co.take<int>(nFaces + 1), o_t2 = co.take<int>(nFaces + 1);
+        const size_t o_tot = co.take<int>(8);
+        SB_CUDA_CHECK(b->order.ensure(co.off));
+        char *ob = b->order.as<char>();
+        FaceOrderArgs fo;
+        fo.nFaces = nFaces;
+        fo.FA = FA;
+        fo.FB = FB;
+        fo.faceTri = faceTri;
+        fo.faceBegin = faceBegin;
+        fo.pairIdx = pairIdx;
+        fo.pairAB = pairAB;
+        fo.A = A;
+        fo.B = B;
+        fo.exact = useRank && A.tnode && B.tnode ? 1 : 0;
+        fo.key = (unsigned long long *)(ob + o_fk);
+        fo.val = (int *)(ob + o_fv);
+        fo.sortedVal = (const int *)(ob + o_fvs);
+        fo.faceRank = (int *)(ob + o_fr);
+        fo.faceByRank = (int *)(ob + o_fbr);
+        fo.insKeys = (uint32_t *)(ob + o_ik);
+        fo.hs[0] = hash_scratch_at((int *)(ob + o_hA), FA);
+        fo.hs[1] = hash_scratch_at((int *)(ob + o_hB), FB);
+        fo.overflow = d_counters + kCntCount; // spare counter slot past the assembly's
+        launch_face_keys(fo, s);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, fo.key, (unsigned long long *)(ob + o_fks), fo.val,
+                                                   (int *)(ob + o_fvs), nFaces, 0, 64, s);
+        }));
+        launch_face_ctx(fo, s);
+        faceRank = fo.faceRank;
+        faceByRank = fo.faceByRank;
+        ptRef = (int *)(ob + o_pr);
+        edgeRef = (int *)(ob + o_er);
+        retriRef = (int *)(ob + o_rr2);
+        rankTmp[0] = (int *)(ob + o_t0);
+        rankTmp[1] = (int *)(ob + o_t1);
+        rankTmp[2] = (int *)(ob + o_t2);
+        rankTot = (int *)(ob + o_tot);
+        RankScanArgs ra;
+        std::memset(&ra, 0, sizeof ra);
+        ra.n = nFaces;
+        ra.FA = FA;
+        ra.count = 2;
+        ra.faceByRank = faceByRank;
+        ra.faceRank = faceRank;
+        ra.vals[0] = ptCap;
+        ra.vals[1] = edgeCap;
+        ra.out[0] = ptRef;
+        ra.out[1] = edgeRef;
+        ra.tmp[0] = rankTmp[0];
+        ra.tmp[1] = rankTmp[1];
+        ra.tot[0] = rankTot;
+        ra.tot[1] = rankTot + 2;
+        launch_rank_scan(ra, s);
         unsigned long long sTot = 0;
         int pTot = 0, tTot = 0, eTot = 0;
         Readback rb(b);
@@ -1017,6 +1084,8 @@ sb_status combine_impl(sb_boolean *b)
     g.edgeOff = edgeOff;
     g.cutPts = cutPts;
     g.cutKeys = cutKeys;
+    g.ptRef = ptRef;
+    g.edgeRef = edgeRef;
     g.faceTris = faceTris;
     g.faceEdges = faceEdges;
     g.counters = d_counters;
@@ -1100,17 +1169,29 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, notB, g.uncutRankB, nB + 1, s);
     }));
-    if (nFaces > 0)
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceNtris, retriRank, nFaces + 1, s);
-        }));
+    if (nFaces > 0) {
+        // the re-triangulated triangles are numbered in the faces' processing order
+        RankScanArgs ra;
+        std::memset(&ra, 0, sizeof ra);
+        ra.n = nFaces;
+        ra.FA = FA;
+        ra.count = 1;
+        ra.faceByRank = faceByRank;
+        ra.faceRank = faceRank;
+        ra.vals[0] = faceNtris;
+        ra.out[0] = retriRank;
+        ra.tmp[0] = rankTmp[2];
+        ra.tot[0] = rankTot + 4;
+        launch_rank_scan(ra, s);
+    }
+    (void)retriRef;
     int cnts[4] = {0, 0, 0, 0}; // uncutA, uncutB, retriA, retri total
     {
         Readback rb(b);
         SB_CUDA_CHECK(rb.add(cnts, g.uncutRankA + nA, sizeof(int)));
         SB_CUDA_CHECK(rb.add(cnts + 1, g.uncutRankB + nB, sizeof(int)));
-        SB_CUDA_CHECK(rb.add(cnts + 2, retriRank + FA, sizeof(int)));
-        SB_CUDA_CHECK(rb.add(cnts + 3, retriRank + nFaces, sizeof(int)));
+        if (nFaces > 0)
+            SB_CUDA_CHECK(rb.add(cnts + 2, rankTot + 4, 2 * sizeof(int)));
         SB_CUDA_CHECK(rb.add(firstFail, d_firstFail, sizeof firstFail));
         SB_CUDA_CHECK(rb.add(&nNew, g.firstRank + nSeq, sizeof nNew));
         SB_CUDA_CHECK(rb.sync());
@@ -1169,11 +1250,14 @@ sb_status combine_impl(sb_boolean *b)
     const uint32_t heCap = pow2_at_least(2 * 3 * (size_t)(g.useAdj ? cnts[3] : nTri) + 2);
     Carve cg2;
     size_t o_ek = cg2.take<uint64_t>(edgeCapH), o_ev = cg2.take<int>(edgeCapH), o_dg = cg2.take<int>(nNew + 1);
+    size_t o_esl = cg2.take<int>(edgeCapH), o_esh = cg2.take<int>(edgeCapH), o_fo = cg2.take<int>(nNew + 1);
+    size_t o_nb = cg2.take<int>(2 * (size_t)nNew + 2), o_nbs = cg2.take<int>(2 * (size_t)nNew + 2);
+    const size_t nQueryCap = (size_t)nTri + 4 * (size_t)nNew + 1;
     size_t o_hkA = cg2.take<uint64_t>(heCap), o_hvA = cg2.take<int>(heCap);
     size_t o_hkB = cg2.take<uint64_t>(heCap), o_hvB = cg2.take<int>(heCap);
     size_t o_par = cg2.take<int>(nTri + 1), o_sf = cg2.take<int>(nTri + 1), o_smn = cg2.take<int>(nTri + 1);
-    size_t o_rmn = cg2.take<int>(nTri + 1), o_ror = cg2.take<int>(nTri + 1), o_rep = cg2.take<int>(nTri + 1);
-    size_t o_ins = cg2.take<int>(nTri + 1);
+    size_t o_rmn = cg2.take<int>(nTri + 1), o_ror = cg2.take<int>(nTri + 1), o_rep = cg2.take<int>(nQueryCap);
+    size_t o_ins = cg2.take<int>(nQueryCap);
 
     SB_CUDA_CHECK(b->groups.ensure(cg2.off));
     char *gb = b->groups.as<char>();
@@ -1181,6 +1265,11 @@ sb_status combine_impl(sb_boolean *b)
     g.edgeVals = (int *)(gb + o_ev);
     g.edgeMask = edgeCapH - 1;
     g.degree = (int *)(gb + o_dg);
+    g.edgeSlotLo = (int *)(gb + o_esl);
+    g.edgeSlotHi = (int *)(gb + o_esh);
+    g.firstOcc = (int *)(gb + o_fo);
+    g.nbr = (int *)(gb + o_nb);
+    g.nbrSlot = (int *)(gb + o_nbs);
     g.heKeysA = (uint64_t *)(gb + o_hkA);
     g.heValsA = (int *)(gb + o_hvA);
     g.heKeysB = (uint64_t *)(gb + o_hkB);
@@ -1191,7 +1280,7 @@ sb_status combine_impl(sb_boolean *b)
     g.seedMin = (int *)(gb + o_smn);
     g.remMin = (int *)(gb + o_rmn);
     g.repOfRoot = (int *)(gb + o_ror);
-    g.reps = (int *)(gb + o_rep);
+    g.qTri = (int *)(gb + o_rep);
     g.insideCount = (int *)(gb + o_ins);
 
     {
@@ -1200,6 +1289,11 @@ sb_status combine_impl(sb_boolean *b)
         fl.u64(g.edgeKeys, edgeCapH, kEmpty64);
         fl.i32(g.edgeVals, edgeCapH, INT_MAX);
         fl.i32(g.degree, (size_t)nNew + 1, 0);
+        fl.i32(g.edgeSlotLo, edgeCapH, INT_MAX);
+        fl.i32(g.edgeSlotHi, edgeCapH, INT_MAX);
+        fl.i32(g.firstOcc, (size_t)nNew + 1, INT_MAX);
+        fl.i32(g.nbr, 2 * (size_t)nNew + 2, -1);
+        fl.i32(g.nbrSlot, 2 * (size_t)nNew + 2, -1);
         fl.u64(g.heKeysA, heCap, kEmpty64);
         fl.u64(g.heKeysB, heCap, kEmpty64);
         fl.i32(g.heValsA, heCap, INT_MAX);
@@ -1209,12 +1303,95 @@ sb_status combine_impl(sb_boolean *b)
             fl.i32(g.seedMin, nTri, INT_MAX);
             fl.i32(g.remMin, nTri, INT_MAX);
             fl.i32(g.repOfRoot, nTri, -1);
-            fl.i32(g.insideCount, (size_t)nTri + 1, 0);
+            fl.i32(g.insideCount, nQueryCap, 0);
         }
         fl.launch();
     }
     launch_loops(g, s);
     launch_groups(g, s);
+    // the loops in the reference's order, the group seeds and each group's first triangle
+    const size_t nNewS = (size_t)std::max(nNew, 1), nTriS = (size_t)std::max(nTri, 1);
+    const int slotDomain = 4 * (int)K; // first-mesh faces hold 2 K directed cut-edge slots, two sequence slots each
+    Carve cl;
+    const size_t o_st = cl.take<int>(4 * nNewS), o_el = cl.take<int>(nNewS), o_fq = cl.take<int>(nTriS);
+    const size_t o_g0 = cl.take<int>(4 * nNewS), o_gq = cl.take<int>(4 * nNewS), o_inf = cl.take<int>(4);
+    const size_t o_lfl = cl.take<int>(loop_order_flag_ints(slotDomain, nNew));
+    const size_t o_irk = cl.take<int>(nNewS), o_itp = cl.take<int>(nNewS), o_lkeys = cl.take<uint32_t>(nNewS);
+    const size_t o_sa = cl.take<int>(2 * nNewS), o_sbb = cl.take<int>(2 * nNewS), o_va = cl.take<int>(2 * nNewS);
+    const size_t o_vb = cl.take<int>(2 * nNewS), o_cy = cl.take<int>(2 * nNewS), o_ll = cl.take<int>(nNewS + 1);
+    const size_t o_ho = cl.take<int>(nNewS), o_lhs = cl.take<int>(hash_scratch_ints(nNew));
+    const size_t o_rsn = cl.take<int>(nTriS), o_rsx = cl.take<int>(nTriS), o_bg = cl.take<int>(nTriS);
+    const size_t o_be = cl.take<int>(nTriS), o_f0 = cl.take<int>(nTriS), o_f1 = cl.take<int>(nTriS);
+    const size_t o_tg = cl.take<int>(3 * nTriS), o_ffl = cl.take<int>(std::max(3 * nTriS, 4 * nNewS) + 1);
+    SB_CUDA_CHECK(b->flood.ensure(cl.off));
+    char *lb = b->flood.as<char>();
+    LoopOrderArgs lo;
+    lo.nNew = nNew;
+    lo.newBase = (uint32_t)g.newBase;
+    lo.slotDomain = slotDomain;
+    lo.degree = g.degree;
+    lo.nbr = g.nbr;
+    lo.nbrSlot = g.nbrSlot;
+    lo.firstOcc = g.firstOcc;
+    lo.loopBad = d_counters + kCntLoopVerts + 1;
+    lo.loopErr = d_counters + kCntSideErrors;
+    lo.heKeysA = g.heKeysA;
+    lo.heKeysB = g.heKeysB;
+    lo.heValsA = g.heValsA;
+    lo.heValsB = g.heValsB;
+    lo.heMask = g.heMask;
+    lo.seedTri = (int *)(lb + o_st);
+    lo.entryLoop = (int *)(lb + o_el);
+    lo.firstQ = (int *)(lb + o_fq);
+    lo.group0 = (int *)(lb + o_g0);
+    lo.gQuery = (int *)(lb + o_gq);
+    lo.qTri = g.qTri;
+    lo.qCount = d_counters + kCntReps;
+    lo.info = (int *)(lb + o_inf);
+    lo.flag = (int *)(lb + o_lfl);
+    lo.insRank = (int *)(lb + o_irk);
+    lo.iterPos = (int *)(lb + o_itp);
+    lo.insKeys = (uint32_t *)(lb + o_lkeys);
+    lo.succA = (int *)(lb + o_sa);
+    lo.succB = (int *)(lb + o_sbb);
+    lo.valA = (int *)(lb + o_va);
+    lo.valB = (int *)(lb + o_vb);
+    lo.cyc = (int *)(lb + o_cy);
+    lo.loopLen = (int *)(lb + o_ll);
+    lo.hashOut = (int *)(lb + o_ho);
+    lo.hs = hash_scratch_at((int *)(lb + o_lhs), nNew);
+    FloodArgs fd;
+    fd.nTri = nTri;
+    fd.nNew = nNew;
+    fd.root = g.parent;
+    fd.seedMin = g.seedMin;
+    fd.seedTri = lo.seedTri;
+    fd.firstQ = lo.firstQ;
+    fd.entryLoop = lo.entryLoop;
+    fd.gQuery = lo.gQuery;
+    fd.info = lo.info;
+    fd.insideCount = g.insideCount;
+    fd.regionQuery = g.repOfRoot;
+    fd.rsMin = (int *)(lb + o_rsn);
+    fd.rsMax = (int *)(lb + o_rsx);
+    fd.bfsGroup = (int *)(lb + o_bg);
+    fd.best = (int *)(lb + o_be);
+    fd.front0 = (int *)(lb + o_f0);
+    fd.front1 = (int *)(lb + o_f1);
+    fd.tgt = (int *)(lb + o_tg);
+    fd.flag = (int *)(lb + o_ffl);
+    fd.errors = d_counters + kCntSideErrors;
+    {
+        Fills fl(s);
+        fl.i32(lo.firstQ, nTriS, INT_MAX);
+        fl.i32(lo.info, 4, 0);
+        fl.i32(fd.rsMin, nTriS, 2);
+        fl.i32(fd.rsMax, nTriS, -1);
+        fl.i32(fd.bfsGroup, nTriS, -1);
+        fl.i32(fd.best, nTriS, INT_MAX);
+        fl.launch();
+    }
+    launch_loop_order(lo, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[5], s));
     unsigned int counters[kCntCount];
@@ -1223,10 +1400,11 @@ sb_status combine_impl(sb_boolean *b)
         if (r != SB_OK)
             return r;
     }
-    const unsigned int nReps = counters[kCntReps];
-    SB_CUDA_CHECK(b->sides.ensure(side_layout(g, 3 * (int)nReps, nullptr)));
-    side_layout(g, 3 * (int)nReps, b->sides.as<char>());
-    launch_sides(g, nReps, fp64, s);
+    const unsigned int nQueries = counters[kCntReps];
+    SB_CUDA_CHECK(b->sides.ensure(side_layout(g, 3 * (int)nQueries, nullptr)));
+    side_layout(g, 3 * (int)nQueries, b->sides.as<char>());
+    launch_sides(g, nQueries, fp64, s);
+    launch_flood_labels(g, fd, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[6], s));
 
@@ -1259,10 +1437,14 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cudaEventRecord(b->ev[7], s));
     unsigned long long dstats[8];
     int runEnd[3] = {0, 0, 0}; // scan values where the three fetch runs end
+    unsigned int orderFallbacks = 0;
+    int loopInfo[2] = {0, 0};
     {
         Readback rb(b);
         SB_CUDA_CHECK(rb.add(dstats, d_stats, sizeof dstats));
         SB_CUDA_CHECK(rb.add(counters, d_counters, sizeof counters));
+        SB_CUDA_CHECK(rb.add(&orderFallbacks, d_counters + kCntCount, sizeof orderFallbacks));
+        SB_CUDA_CHECK(rb.add(loopInfo, lo.info, sizeof loopInfo));
         if (status == SB_OK && nTri > 0)
             for (int op = 0; op < 3; ++op)
                 SB_CUDA_CHECK(rb.add(runEnd + op, fRank + op * ((size_t)nTri + 1) + nTri, sizeof(int)));
@@ -1292,6 +1474,8 @@ sb_status combine_impl(sb_boolean *b)
     st.loop_vertices = counters[kCntLoopVerts];
     st.loop_bad_degree = counters[kCntLoopVerts + 1];
     st.duplicate_halfedges = counters[kCntDupHalfedge];
+    st.loops = (uint32_t)loopInfo[1];
+    st.order_fallbacks = orderFallbacks;
     for (int k = 0; k < 7; ++k) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, b->ev[k], b->ev[k + 1]);
@@ -1726,7 +1910,7 @@ void sb_boolean_destroy(sb_boolean *b)
     if (!b)
         return;
     for (DevBuf *d : {&b->cand, &b->isect, &b->faces, &b->scratch, &b->cut, &b->weld, &b->arr, &b->groups, &b->res,
-                      &b->cub, &b->small, &b->trunc, &b->sides})
+                      &b->cub, &b->small, &b->trunc, &b->sides, &b->order, &b->flood})
         d->release();
     if (b->evInit)
         for (auto &e : b->ev)

@@ -590,13 +590,17 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
     }
     res.ntris = nTris;
 
-    // ---- cut edges (undirected, both ends local ids) ---------------------------------------------------
+    // ---- cut edges: the neighbour map walked as the reference's reTriangulate lambda walks it
+    // (src/solidboolean.cpp:397-404): keys in the library's iteration order, each key's set in its order, as
+    // directed (from, to) pairs of local ids; every undirected edge appears once from each end. The global
+    // cut-loop map is built from this sequence, so its order decides where each loop starts.
     int ne = 0;
-    for (int i = 0; i < m; ++i) {
-        const int *nb = s.raw + s.rawOff[i];
-        for (int r = 0; r < s.nbrCnt[i]; ++r)
-            if (nb[r] > 3 + i && ne < np) {
-                outEdges[2 * ne] = 3 + i;
+    for (int q = 0; q < nt; ++q) {
+        const int from = s.outer[q];
+        const int *nb = s.raw + s.rawOff[from - 3];
+        for (int r = 0; r < s.nbrCnt[from - 3]; ++r)
+            if (ne < 2 * np) {
+                outEdges[2 * ne] = from;
                 outEdges[2 * ne + 1] = nb[r];
                 ++ne;
             }
@@ -639,7 +643,7 @@ __global__ void k_face_sizes(int nFaces, const int *__restrict__ faceBegin, unsi
     scratchBytes[f] = (unsigned long long)face_scratch_bytes_dev(np);
     ptCap[f] = 2 * np;
     triCap[f] = 32 * np + 16;
-    edgeCap[f] = np;
+    edgeCap[f] = 2 * np; // directed: each undirected edge from both ends
 }
 
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,

@@ -22,7 +22,8 @@ struct FaceArgs {
     d3 *cutPts;
     Key *cutKeys;
     int *faceTris;                             // local ids, 3 per triangle
-    int *faceEdges;                            // local ids, 2 per edge
+    int *faceEdges;                            // directed cut edges (local ids, 2 per edge) in the face's
+                                               // neighbour-map iteration order, both directions
     int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
     int *ptSrc = nullptr; // optional, per face point: 2 x (intersecting pair) + segment end it came from
 };

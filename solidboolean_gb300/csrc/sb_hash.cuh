@@ -29,6 +29,23 @@ __device__ __forceinline__ void u64map_insert_min(uint64_t *keys, int *vals, uin
     }
 }
 
+// map key -> min(value), returning the key's slot (-1 when the table is full)
+__device__ __forceinline__ int u64map_insert_min_slot(uint64_t *keys, int *vals, uint32_t mask, uint64_t key,
+                                                      int val)
+{
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint64_t prev = atomicCAS((unsigned long long *)(keys + s), (unsigned long long)kEmpty64,
+                                        (unsigned long long)key);
+        if (prev == kEmpty64 || prev == key) {
+            atomicMin(vals + s, val);
+            return (int)s;
+        }
+        s = (s + 1) & mask;
+    }
+    return -1;
+}
+
 // value of key, or -1
 __device__ __forceinline__ int u64map_find(const uint64_t *keys, const int *vals, uint32_t mask, uint64_t key)
 {

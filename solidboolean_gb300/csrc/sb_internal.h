@@ -51,6 +51,10 @@ struct MeshDev {
     double *nbox64 = nullptr; // [(nt-1)*6]
     int *flags = nullptr;     // [nt-1] refit arrival counters
     int *rank = nullptr;      // [nt] position of each triangle in the reference tree's leaf order
+    // the reference tree's nodes: {first leaf position, member count, left child id (the right child is
+    // left + 1), -1 for a leaf}; node 0 is the root. Valid with rank.
+    int4 *tnode = nullptr;
+    int tnodeCount = 0;       // records the node table holds
     bool rankValid = false;
     // [nt*3] for edge k of triangle i (t[k] -> t[k+1]): the first triangle in index order holding the reverse
     // edge, -1 for none. Depends on the triangles only, so a vertex update keeps it.

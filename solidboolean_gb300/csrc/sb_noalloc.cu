@@ -73,7 +73,7 @@ __global__ void k_na_setup(int nFaces, int nSeg, const int *__restrict__ segBegi
     if (f == nFaces) {
         ptOff[f] = 2 * nSeg;
         triOff[f] = nFaces * triCap;
-        edgeOff[f] = nSeg;
+        edgeOff[f] = 2 * nSeg;
         scratchBytes[f] = 0;
         if (segBegin[nFaces] != nSeg || segBegin[0] != 0)
             atomicOr(invalid, 1);
@@ -89,7 +89,7 @@ __global__ void k_na_setup(int nFaces, int nSeg, const int *__restrict__ segBegi
     cornerTris[3 * f + 2] = 3u * f + 2u;
     ptOff[f] = 2 * b;
     triOff[f] = f * triCap;
-    edgeOff[f] = b;
+    edgeOff[f] = 2 * b;
 }
 
 } // namespace sbg
@@ -131,7 +131,7 @@ extern "C" sb_status sb_retriangulate_faces_noalloc(const double *d_corners, con
     size_t o_side = c.take<int>(n_faces + 1), o_tri = c.take<int>(n_faces + 1);
     size_t o_pidx = c.take<int>(n_segments + 1), o_ct = c.take<uint32_t>(3 * (size_t)n_faces);
     size_t o_po = c.take<int>(n_faces + 1), o_to = c.take<int>(n_faces + 1), o_eo = c.take<int>(n_faces + 1);
-    size_t o_keys = c.take<Key>(2 * (size_t)n_segments + 1), o_edges = c.take<int>(2 * (size_t)n_segments + 2);
+    size_t o_keys = c.take<Key>(2 * (size_t)n_segments + 1), o_edges = c.take<int>(4 * (size_t)n_segments + 2);
     size_t o_ne = c.take<int>(n_faces + 1);
     size_t o_c1 = c.take<int>(n_faces + 1), o_c2 = c.take<int>(n_faces + 1), o_c3 = c.take<int>(n_faces + 1);
     const size_t fixedBytes = c.off;

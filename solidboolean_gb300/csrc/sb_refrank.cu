@@ -56,6 +56,7 @@ enum {
     kCtFirst = 4,   // current level: first node
     kCtLast = 5,    //                one past the last node
     kCtSubErr = 6,  // subtree blocks that ran out of node records
+    kCtTNodes = 7,  // node-table records allocated (subtree nodes are numbered from maxNodes up)
     kCtCount = 8
 };
 
@@ -987,10 +988,20 @@ __global__ void __launch_bounds__(kElemThreads, 4)
 
 // After the last level: every member's terminal node, and the sort key (the node's first leaf position)
 // stored by triangle index, so that a stable sort lists each node's members by ascending index.
+// It also starts the tree's node table with the large nodes: {first leaf position, member count, left child
+// (right = left + 1), or -1 while the node is terminal}; the subtree blocks fill in the terminal nodes' own
+// subtrees, numbering their nodes from maxNodes up.
 __global__ void k_rr_finish(int nt, const int *__restrict__ state, const NParam *__restrict__ np,
-                            const RNode *__restrict__ nodes, const int *__restrict__ leafTri, int *key, int *val)
+                            const RNode *__restrict__ nodes, const int *__restrict__ leafTri, int *key, int *val,
+                            int4 *tnode, int *counters, int maxNodes)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < min(counters[kCtNodes], maxNodes)) {
+        const int cnt = nodes[q].count;
+        tnode[q] = make_int4(nodes[q].begin, cnt, cnt > kSub ? np[q].child : -1, 0);
+    }
+    if (q == 0)
+        counters[kCtTNodes] = maxNodes;
     if (q >= nt)
         return;
     const int v = state[q];
@@ -1037,7 +1048,8 @@ constexpr size_t kSubSmem = sizeof(SNode) * kSubNodes + sizeof(int) * (6 * kSub 
 __device__ __forceinline__ void subtree_one(int t, const int *__restrict__ terms, const RNode *__restrict__ gnodes,
                                             const int *__restrict__ sorted, const RRec *__restrict__ rec,
                                             const int *__restrict__ posOf, const int *__restrict__ leafTri,
-                                            const int *__restrict__ scg, int *rank, int *counters)
+                                            const int *__restrict__ scg, int *rank, int *counters, int4 *tnode,
+                                            int tnodeCap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     SNode *nodes = reinterpret_cast<SNode *>(smem);
@@ -1046,7 +1058,7 @@ __device__ __forceinline__ void subtree_one(int t, const int *__restrict__ terms
     int *flag = reinterpret_cast<int *>(smem + sizeof(SNode) * kSubNodes + sizeof(int) * 4 * kSub);
     int *scan = flag + kSub;
     int *warpSum = scan + kSub + 1;
-    __shared__ int nNodes, lFirst, lLast, anyAmb, err;
+    __shared__ int nNodes, lFirst, lLast, anyAmb, err, tBase;
     const int tid = threadIdx.x;
     const RNode &g = gnodes[terms[t]];
     const int base = g.begin, n = g.count, dir = g.dir;
@@ -1300,6 +1312,22 @@ __device__ __forceinline__ void subtree_one(int t, const int *__restrict__ terms
         atomicAdd(counters + kCtSubErr, 1);
     for (int p = tid; p < n; p += kSubThreads)
         rank[leafTri[perm[cur][p]]] = base + p;
+    // the subtree's nodes in the node table: record k > 0 becomes tBase + k - 1 (children stay adjacent)
+    if (tid == 0) {
+        tBase = atomicAdd(counters + kCtTNodes, nNodes - 1);
+        if (tBase + nNodes - 1 > tnodeCap)
+            atomicAdd(counters + kCtSubErr, 1);
+    }
+    __syncthreads();
+    if (tBase + nNodes - 1 <= tnodeCap)
+        for (int k = tid; k < nNodes; k += kSubThreads) {
+            const SNode &nd = nodes[k];
+            const int left = (nd.child >= 0 && nd.count > kLeaf) ? tBase + nd.child - 1 : -1;
+            if (k == 0)
+                tnode[terms[t]].z = left;
+            else
+                tnode[tBase + k - 1] = make_int4(base + nd.begin, nd.count, left, 0);
+        }
 }
 
 // The terminal nodes, a block at a time: the count is known only on the device, so the grid is one resident
@@ -1307,11 +1335,11 @@ __device__ __forceinline__ void subtree_one(int t, const int *__restrict__ terms
 __global__ void __launch_bounds__(kSubThreads, 4)
     k_rr_subtree(const int *__restrict__ terms, const RNode *__restrict__ gnodes, const int *__restrict__ sorted,
                  const RRec *__restrict__ rec, const int *__restrict__ posOf, const int *__restrict__ leafTri,
-                 const int *__restrict__ scg, int *rank, int *counters)
+                 const int *__restrict__ scg, int *rank, int *counters, int4 *tnode, int tnodeCap)
 {
     const int nTerms = counters[kCtTerms];
     for (int t = blockIdx.x; t < nTerms; t += gridDim.x) {
-        subtree_one(t, terms, gnodes, sorted, rec, posOf, leafTri, scg, rank, counters);
+        subtree_one(t, terms, gnodes, sorted, rec, posOf, leafTri, scg, rank, counters, tnode, tnodeCap);
         __syncthreads(); // shared memory is reused by the next node
     }
 }
@@ -1571,6 +1599,9 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     const size_t o_np = c.take<NParam>(maxNodes);
     const size_t o_nodes = c.take<RNode>(maxNodes), o_terms = c.take<int>(maxNodes), o_ct = c.take<int>(kCtCount),
                  o_sc = c.take<int>(4), o_bar = c.take<GridBar>(1), o_cub = c.take<char>(sortBytes);
+    // node table: the large nodes (ids below maxNodes) and at most 2 nt subtree nodes
+    const int tnodeCap = maxNodes + 2 * nt + 2;
+    const size_t o_tn = c.take<int4>(tnodeCap);
     SB_CUDA_CHECK(m->rankTmp.ensure(c.off));
     char *b = m->rankTmp.as<char>();
     RRec *rec = (RRec *)(b + o_rec);
@@ -1582,6 +1613,9 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     RNode *nodes = (RNode *)(b + o_nodes);
     int *terms = (int *)(b + o_terms), *counters = (int *)(b + o_ct), *scg = (int *)(b + o_sc);
     GridBar *bar = (GridBar *)(b + o_bar);
+    int4 *tnode = (int4 *)(b + o_tn);
+    d.tnode = tnode;
+    d.tnodeCount = tnodeCap;
 
     const int GE = (nt + kElemThreads - 1) / kElemThreads;
     SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters, reinterpret_cast<unsigned *>(bar));
@@ -1611,7 +1645,8 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
         }
         SB_CUDA_CHECK(coop_hold(dev, topBlocks, s));
     }
-    SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val);
+    SB_COUNT(k_rr_finish)<<<GE, kElemThreads, 0, s>>>(nt, state, np, nodes, d.leafTri, key, val, tnode, counters,
+                                                       maxNodes);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(b + o_cub, sortBytes, key, skey, val, sval, nt, 0, keyBits, s));
     {
         static std::once_flag smemOnce; // a per-call attribute set is a driver call every build
@@ -1625,7 +1660,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     {
         KTime kt("k_rr_subtree", s);
         SB_COUNT(k_rr_subtree)<<<std::min(maxNodes, subtree_grid()), kSubThreads, kSubSmem, s>>>(terms, nodes, sval, rec, posOf, d.leafTri,
-                                                                        scg, d.rank, counters);
+                                                                        scg, d.rank, counters, tnode, tnodeCap);
     }
     // counters and barrier record to pinned host memory; read now, or by reference_rank_result once the
     // caller has synchronised past this stream

@@ -67,8 +67,11 @@ def sorted_pairs(p: np.ndarray) -> np.ndarray:
 
 
 def compare(oracle: dict, gpu: dict, n_orig: int, factor: int, coord_rtol: float = 1e-12,
-            check_labels: bool = True) -> dict:
-    """Returns a dict of named mismatches (empty when the results agree)."""
+            check_labels: bool = True, strict: bool = False) -> dict:
+    """Returns a dict of named mismatches (empty when the results agree).
+
+    strict: also the reference's own numbering and order, element by element: the result vertices (ids and
+    bit-exact coordinates), the arrangement's triangles in m_newTriangles order, and each triangle's label."""
     bad: dict = {}
     if oracle["status"] != gpu["status"]:
         bad["status"] = (oracle["status"], gpu["status"])
@@ -124,6 +127,18 @@ def compare(oracle: dict, gpu: dict, n_orig: int, factor: int, coord_rtol: float
         lg = labelled_tris(gpu["newt"], gpu["labels"], rg)
         if lo.shape != lg.shape or not np.array_equal(lo, lg):
             bad["labels"] = (len(lo), len(lg))
+    if strict:
+        ov, gv = np.asarray(oracle["newv"]), np.asarray(gpu["newv"])
+        if ov.shape != gv.shape or not np.array_equal(ov.view(np.int64), gv.view(np.int64)):
+            bad["strict_vertices"] = int(np.count_nonzero(np.any(ov != gv, axis=1))) if ov.shape == gv.shape else -1
+        ot, gt = np.asarray(oracle["newt"]).reshape(-1, 3), np.asarray(gpu["newt"]).reshape(-1, 3)
+        if ot.shape != gt.shape or not np.array_equal(ot, gt):
+            bad["strict_arrangement"] = int(np.count_nonzero(np.any(ot != gt, axis=1))) if ot.shape == gt.shape else -1
+        elif check_labels:
+            ol = oracle_labels(oracle)
+            gl = np.asarray(gpu["labels"]).astype(np.int64)
+            if not np.array_equal(ol, gl):
+                bad["strict_labels"] = int(np.count_nonzero(ol != gl))
     return bad
 
 

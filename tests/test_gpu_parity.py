@@ -1,4 +1,8 @@
-"""GPU results against the oracle restatement of the reference path, through the C ABI."""
+"""GPU results against the oracle restatement of the reference path, through the C ABI.
+
+Strict parity: besides the canonical comparisons, the result vertices (ids and bit-exact coordinates), the
+arrangement's triangles in the reference's m_newTriangles order and every triangle's label equal the
+oracle's element by element."""
 import numpy as np
 import pytest
 
@@ -39,8 +43,9 @@ def test_parity(gpu_lib, port, case, precision):
     va, fa, vb, fb = CASES[case]()
     ref = port.run(va, fa, vb, fb, 100000)
     got = sbg.run_boolean(va, fa, vb, fb, 100000, precision)
-    bad = compare(ref, got, len(va) + len(vb), 100000)
+    bad = compare(ref, got, len(va) + len(vb), 100000, strict=True)
     assert not bad, (case, precision, bad, got["stats"])
+    assert got["stats"]["order_fallbacks"] == 0
 
 
 @pytest.mark.parametrize("case", ["pair_small", "pair_large_L5", "near_tangent_L5", "batch"])

@@ -13,8 +13,9 @@ pytestmark = pytest.mark.gpu
 def _check(port, va, fa, vb, fb, q, precision="filtered"):
     ref = port.run(va, fa, vb, fb, q)
     got = sbg.run_boolean(va, fa, vb, fb, q, precision)
-    bad = compare(ref, got, len(va) + len(vb), q)
+    bad = compare(ref, got, len(va) + len(vb), q, strict=True)
     assert not bad, (bad, got["stats"])
+    assert got["stats"]["order_fallbacks"] == 0
     return ref, got
 
 
@@ -38,22 +39,14 @@ def test_near_tangent_L6(gpu_lib, port):
     _check(port, va, fa, vb, fb, 100000)
 
 
-def test_diff_volume_L5_with_offsets_topology(gpu_lib, port):
-    """Pairs, segments, vertices and the arrangement's triangles bit-exact on a leaky arrangement (the cut
-    loops do not close every region)."""
+@pytest.mark.parametrize("weld", [100000, 100000000])
+def test_diff_volume_L5_with_offsets(gpu_lib, port, weld):
+    """A leaky arrangement (the cut loops do not close every region, so some flood regions hold groups the
+    reference decides differently): labels follow the reference's first-in-first-out flood in the
+    iteration order of its hash containers, triangle for triangle."""
     va, fa, vb, fb, off = mg.diff_volume(1234, 5)
-    ref = port.run(va, fa, vb + off, fb, 100000)
-    got = sbg.run_boolean(va, fa, vb + off, fb, 100000)
-    bad = compare(ref, got, len(va) + len(vb), 100000, check_labels=False)
-    assert not bad, (bad, got["stats"])
-
-
-@pytest.mark.xfail(strict=True, reason="labels of a leaky arrangement: the reference floods regions in the "
-                   "iteration order of its hash containers across the whole mesh; a few dozen triangles of "
-                   "regions that the cut loops do not close get the other side")
-def test_diff_volume_L5_with_offsets_labels(gpu_lib, port):
-    va, fa, vb, fb, off = mg.diff_volume(1234, 5)
-    _check(port, va, fa, vb + off, fb, 100000)
+    ref, got = _check(port, va, fa, vb + off, fb, weld)
+    assert ref["status"] == 1 and got["stats"]["loops"] > 1
 
 
 @pytest.mark.parametrize("precision", ["filtered", "fp64"])
