@@ -125,8 +125,9 @@ sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t 
  * "arrangement" (uint32 triangles), "labels" (int8 per arrangement triangle: 0 outside, 1 inside, -1 in no
  * group), "tri_mesh" (int8 per arrangement triangle: 0 first mesh, 1 second), "new_sources" (int32 per
  * appended result vertex: 2 x its intersecting pair + the end of that pair's segment it was built from),
- * "rank_first" / "rank_second" (int32 per triangle: position in the reference tree's leaf order). *bytes
- * receives the size; out may be NULL. */
+ * "rank_first" / "rank_second" (int32 per triangle: position in the reference tree's leaf order),
+ * "loop_order_ns" (8 uint64: device time stamps at the phase boundaries of the loop-order stage, a
+ * diagnostic). *bytes receives the size; out may be NULL. */
 sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
 void sb_boolean_destroy(sb_boolean *b);
 

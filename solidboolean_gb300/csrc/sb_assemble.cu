@@ -415,28 +415,6 @@ __global__ void k_region_rep(int nTri, const int *__restrict__ root, const int *
     }
 }
 
-// Regions without seeds are the reference's remaining groups (src/solidboolean.cpp:231-238): each is flooded
-// from its smallest uncut triangle, whose side is queried; regions with seeds take their groups' sides.
-__global__ void k_region_list(int nTri, const int *__restrict__ root, const int *__restrict__ seedMin,
-                              const int *__restrict__ remMin, int *regionQuery, int *qTri, unsigned int *nQueries,
-                              const int8_t *__restrict__ triMesh, unsigned int *regionsPerMesh)
-{
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nTri || root[t] != t)
-        return;
-    regionQuery[t] = -1;
-    if (seedMin[t] != INT_MAX) {
-        atomicAdd(regionsPerMesh + triMesh[t], 1u);
-        return;
-    }
-    if (remMin[t] != INT_MAX) {
-        unsigned int k = atomicAdd(nQueries, 1u);
-        qTri[k] = remMin[t];
-        regionQuery[t] = (int)k;
-        atomicAdd(regionsPerMesh + triMesh[t], 1u);
-    }
-}
-
 // isPointInMesh (src/solidboolean.cpp:48-92) for one (region, axis) per warp: the 32 lanes pop up to 32
 // LBVH nodes at a time from a per-warp shared-memory stack, test the children against the ray's box
 // (FP32 boxes rounded outward, or exact FP64 boxes in the plain form), test reached triangles exactly in
@@ -931,12 +909,6 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
     {
         KTime kt("k_region_rep", s);
         SB_COUNT(k_region_rep)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedFlag, g.isUncut, g.seedMin, g.remMin);
-    }
-    {
-        KTime kt("k_region_list", s);
-        SB_COUNT(k_region_list)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.parent, g.seedMin, g.remMin, g.repOfRoot,
-                                                                g.qTri, g.counters + kCntReps, g.triMesh,
-                                                                g.counters + kCntRegionsA);
     }
 }
 

@@ -611,6 +611,7 @@ struct sb_boolean {
     cudaEvent_t ev[10];
     cudaStream_t side = nullptr;     // second stream for preparing the two meshes concurrently
     cudaEvent_t sideDone = nullptr;
+    cudaEvent_t orderDone = nullptr; // the cut faces' processing order, computed on `side`
     bool evInit = false;
     char *mail = nullptr; // pinned mailbox: small reads [0, kMailRead), constant uploads after it
 };
@@ -924,6 +925,7 @@ sb_status combine_impl(sb_boolean *b)
     long long totals[4] = {0, 0, 0, 0};
     int *faceRank = nullptr, *faceByRank = nullptr, *ptRef = nullptr, *edgeRef = nullptr, *retriRef = nullptr;
     int *rankTmp[3] = {nullptr, nullptr, nullptr}, *rankTot = nullptr;
+    bool orderPending = false;
     if (nFaces > 0) {
         SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
@@ -975,12 +977,6 @@ sb_status combine_impl(sb_boolean *b)
         fo.hs[0] = hash_scratch_at((int *)(ob + o_hA), FA);
         fo.hs[1] = hash_scratch_at((int *)(ob + o_hB), FB);
         fo.overflow = d_counters + kCntCount; // spare counter slot past the assembly's
-        launch_face_keys(fo, s);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRadixSort::SortPairs(tmp, bytes, fo.key, (unsigned long long *)(ob + o_fks), fo.val,
-                                                   (int *)(ob + o_fvs), nFaces, 0, 64, s);
-        }));
-        launch_face_ctx(fo, s);
         faceRank = fo.faceRank;
         faceByRank = fo.faceByRank;
         ptRef = (int *)(ob + o_pr);
@@ -1005,7 +1001,6 @@ sb_status combine_impl(sb_boolean *b)
         ra.tmp[1] = rankTmp[1];
         ra.tot[0] = rankTot;
         ra.tot[1] = rankTot + 2;
-        launch_rank_scan(ra, s);
         unsigned long long sTot = 0;
         int pTot = 0, tTot = 0, eTot = 0;
         Readback rb(b);
@@ -1018,6 +1013,25 @@ sb_status combine_impl(sb_boolean *b)
         totals[1] = pTot;
         totals[2] = tTot;
         totals[3] = eTot;
+        // the processing order runs on the second stream beside the re-triangulation (the weld waits for it)
+        if (!b->side) {
+            SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+            SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->sideDone, cudaEventDisableTiming));
+        }
+        if (!b->orderDone)
+            SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->orderDone, cudaEventDisableTiming));
+        cudaStream_t so = b->side;
+        SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
+        SB_CUDA_CHECK(cudaStreamWaitEvent(so, b->sideDone, 0));
+        launch_face_keys(fo, so);
+        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+            return cub::DeviceRadixSort::SortPairs(tmp, bytes, fo.key, (unsigned long long *)(ob + o_fks), fo.val,
+                                                   (int *)(ob + o_fvs), nFaces, 0, 64, so);
+        }));
+        launch_face_ctx(fo, so);
+        launch_rank_scan(ra, so);
+        SB_CUDA_CHECK(cudaEventRecord(b->orderDone, so));
+        orderPending = true;
     }
     Carve cu;
     size_t o_cp = cu.take<d3>(totals[1] + 1), o_ck = cu.take<Key>(totals[1] + 1);
@@ -1116,6 +1130,8 @@ sb_status combine_impl(sb_boolean *b)
         fl.i32(g.isFirst, nSeq + 1, 0);
         fl.launch();
     }
+    if (orderPending)
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, b->orderDone, 0));
     launch_weld(g, s);
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, g.isFirst, g.firstRank, (int)nSeq + 1, s);
@@ -1315,11 +1331,10 @@ sb_status combine_impl(sb_boolean *b)
     Carve cl;
     const size_t o_st = cl.take<int>(4 * nNewS), o_el = cl.take<int>(nNewS), o_fq = cl.take<int>(nTriS);
     const size_t o_g0 = cl.take<int>(4 * nNewS), o_gq = cl.take<int>(4 * nNewS), o_inf = cl.take<int>(4);
-    const size_t o_lfl = cl.take<int>(loop_order_flag_ints(slotDomain, nNew));
-    const size_t o_irk = cl.take<int>(nNewS), o_itp = cl.take<int>(nNewS), o_lkeys = cl.take<uint32_t>(nNewS);
-    const size_t o_sa = cl.take<int>(2 * nNewS), o_sbb = cl.take<int>(2 * nNewS), o_va = cl.take<int>(2 * nNewS);
-    const size_t o_vb = cl.take<int>(2 * nNewS), o_cy = cl.take<int>(2 * nNewS), o_ll = cl.take<int>(nNewS + 1);
+    const size_t o_lsc = cl.take<int>(loop_order_scratch_ints(slotDomain, nNew));
+    const size_t o_irk = cl.take<int>(nNewS), o_lkeys = cl.take<uint32_t>(nNewS), o_vis = cl.take<int2>(2 * nNewS);
     const size_t o_ho = cl.take<int>(nNewS), o_lhs = cl.take<int>(hash_scratch_ints(nNew));
+    const size_t o_eb = cl.take<int>(nNewS), o_en = cl.take<int>(nNewS);
     const size_t o_rsn = cl.take<int>(nTriS), o_rsx = cl.take<int>(nTriS), o_bg = cl.take<int>(nTriS);
     const size_t o_be = cl.take<int>(nTriS), o_f0 = cl.take<int>(nTriS), o_f1 = cl.take<int>(nTriS);
     const size_t o_tg = cl.take<int>(3 * nTriS), o_ffl = cl.take<int>(std::max(3 * nTriS, 4 * nNewS) + 1);
@@ -1327,6 +1342,7 @@ sb_status combine_impl(sb_boolean *b)
     char *lb = b->flood.as<char>();
     LoopOrderArgs lo;
     lo.nNew = nNew;
+    lo.nTri = nTri;
     lo.newBase = (uint32_t)g.newBase;
     lo.slotDomain = slotDomain;
     lo.degree = g.degree;
@@ -1348,18 +1364,16 @@ sb_status combine_impl(sb_boolean *b)
     lo.qTri = g.qTri;
     lo.qCount = d_counters + kCntReps;
     lo.info = (int *)(lb + o_inf);
-    lo.flag = (int *)(lb + o_lfl);
+    lo.scratch = (int *)(lb + o_lsc);
     lo.insRank = (int *)(lb + o_irk);
-    lo.iterPos = (int *)(lb + o_itp);
     lo.insKeys = (uint32_t *)(lb + o_lkeys);
-    lo.succA = (int *)(lb + o_sa);
-    lo.succB = (int *)(lb + o_sbb);
-    lo.valA = (int *)(lb + o_va);
-    lo.valB = (int *)(lb + o_vb);
-    lo.cyc = (int *)(lb + o_cy);
-    lo.loopLen = (int *)(lb + o_ll);
+    lo.vis = (int2 *)(lb + o_vis);
     lo.hashOut = (int *)(lb + o_ho);
     lo.hs = hash_scratch_at((int *)(lb + o_lhs), nNew);
+    lo.entryBase = (int *)(lb + o_eb);
+    lo.entryNext = (int *)(lb + o_en);
+    lo.smemInts = 0;
+    lo.stamps = reinterpret_cast<unsigned long long *>(b->small.as<char>() + 1024); // [8] after the counters
     FloodArgs fd;
     fd.nTri = nTri;
     fd.nNew = nNew;
@@ -1392,6 +1406,7 @@ sb_status combine_impl(sb_boolean *b)
         fl.launch();
     }
     launch_loop_order(lo, s);
+    launch_side_queries(g, lo, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[5], s));
     unsigned int counters[kCntCount];
@@ -1882,6 +1897,10 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
         // per appended vertex: 2 x (its intersecting pair) + (which end of that pair's segment)
         sz = sizeof(int) * (b->nNewV - (size_t)b->newBase);
         src = b->d_newSrc;
+    } else if (n == "loop_order_ns") {
+        // device time stamps (ns) at the phase boundaries of the loop-order kernel of the last combine
+        sz = sizeof(unsigned long long) * 8;
+        src = b->small.as<char>() + 1024;
     } else if (n == "rank_first" || n == "rank_second") {
         const MeshDev &M = n == "rank_first" ? b->first->d : b->second->d;
         sz = M.rankValid ? sizeof(int) * (size_t)M.nt : 0;
@@ -1915,6 +1934,8 @@ void sb_boolean_destroy(sb_boolean *b)
     if (b->evInit)
         for (auto &e : b->ev)
             cudaEventDestroy(e);
+    if (b->orderDone)
+        cudaEventDestroy(b->orderDone);
     if (b->side) {
         cudaStreamDestroy(b->side);
         cudaEventDestroy(b->sideDone);

@@ -21,6 +21,7 @@
 // aligned), then the two positions inside the leaves, order pairs as the traversal emits them.
 #include <algorithm>
 #include <climits>
+#include <mutex>
 
 #include "sb_ktime.h"
 #include "sb_order.cuh"
@@ -81,7 +82,7 @@ __device__ int block_excl_scan(int *a, int n)
 size_t hash_scratch_ints(int n)
 {
     const size_t N = (size_t)std::max(n, 1);
-    return 6 * N + 1 + 3 * (size_t)hash_bucket_count((uint32_t)N) + 8;
+    return 6 * N + 1 + 2 * (size_t)hash_bucket_count((uint32_t)N) + 8;
 }
 
 HashScratch hash_scratch_at(int *base, int n)
@@ -94,65 +95,116 @@ HashScratch hash_scratch_at(int *base, int n)
     h.slotOf = h.posB + N;
     h.nxt = h.slotOf + N;
     h.runSize = h.nxt + N;
-    h.firstOld = h.runSize + 2 * N + 1;
-    h.createNew = h.firstOld + B;
-    h.head = h.createNew + B;
+    h.bmin = h.runSize + 2 * N + 1;
+    h.head = h.bmin + B;
     return h;
 }
 
-// keys[i]: the i-th inserted key (distinct); out[i]: its position in the container's iteration order
-__device__ void hash_order_block(const uint32_t *keys, int n, int *out, HashScratch w)
+// One stage: M elements (the first Mprev of them placed by the previous stage at pos[]) in B buckets ->
+// npos[]. Per bucket, the smallest of (old element: its old position; new element i: Mprev + i) tells both
+// whether the bucket holds old elements and the run's key. bkt[] keeps each element's bucket for the stage.
+__device__ void hash_stage(const uint32_t *keys, int M, int Mprev, uint32_t B, const int *pos, int *npos,
+                           int *bkt, int *nxt, int *runSize, int *bmin, int *head)
+{
+    const int T = blockDim.x, tid = threadIdx.x;
+    for (uint32_t b = tid; b < B; b += T) {
+        bmin[b] = INT_MAX;
+        head[b] = -1;
+    }
+    for (int i = tid; i < M + Mprev; i += T)
+        runSize[i] = 0;
+    __syncthreads();
+    for (int i = tid; i < M; i += T) {
+        const int b = (int)(keys[i] % B);
+        bkt[i] = b;
+        atomicMin(&bmin[b], i < Mprev ? pos[i] : Mprev + i);
+        nxt[i] = atomicExch(&head[b], i);
+    }
+    __syncthreads();
+    // runs: opened by this stage's inserts [0, M - Mprev), latest first; rebuilt [M, M + Mprev)
+    for (int i = tid; i < M; i += T) {
+        const int v = bmin[bkt[i]];
+        atomicAdd(&runSize[v < Mprev ? M + (Mprev - 1 - v) : (M - 1 - (v - Mprev))], 1);
+    }
+    __syncthreads();
+    block_excl_scan(runSize, M + Mprev);
+    for (int i = tid; i < M; i += T) {
+        const int b = bkt[i];
+        const int v = bmin[b];
+        const int slot = v < Mprev ? M + (Mprev - 1 - v) : (M - 1 - (v - Mprev));
+        const int gi = i < Mprev ? 1 : 0;
+        const int ki = gi ? (Mprev - 1 - pos[i]) : (M - 1 - i);
+        int within = 0;
+        for (int j = head[b]; j >= 0; j = nxt[j]) {
+            if (j == i)
+                continue;
+            const int gj = j < Mprev ? 1 : 0;
+            const int kj = gj ? (Mprev - 1 - pos[j]) : (M - 1 - j);
+            within += (gj < gi || (gj == gi && kj < ki)) ? 1 : 0;
+        }
+        npos[i] = runSize[slot] + within;
+    }
+    __syncthreads();
+}
+
+// keys[i]: the i-th inserted key (distinct); out[i]: its position in the container's iteration order. The
+// keys and the stages whose arrays fit in smem (smemInts ints of shared memory) run there; the later stages
+// in w.
+__device__ void hash_order_block(const uint32_t *keysIn, int n, int *out, HashScratch w, int *smem, int smemInts)
 {
     const int T = blockDim.x, tid = threadIdx.x;
     if (n <= 0)
         return;
-    int *pos = w.posA, *npos = w.posB;
+    // keys cached in shared memory when they fit with room to spare
+    const bool keysS = 2ll * n <= (long long)smemInts;
+    const uint32_t *keys = keysIn;
+    if (keysS) {
+        uint32_t *k = reinterpret_cast<uint32_t *>(smem);
+        for (int i = tid; i < n; i += T)
+            k[i] = keysIn[i];
+        keys = k;
+        smem += (n + 3) & ~3;
+        smemInts -= (n + 3) & ~3;
+        __syncthreads();
+    }
+    // the largest stage whose arrays fit: two position buffers, buckets, links, runs (2 M + 1), 2 B per bucket
+    int capM = 0;
+    uint32_t capB = 0;
+    {
+        int mp = 0;
+        for (int st = 0; st < 64; ++st) {
+            const uint32_t Bs = hash_bucket_count((uint32_t)mp + 1);
+            const int Ms = (uint32_t)n < Bs ? n : (int)Bs;
+            if (6ll * Ms + 1 + 2ll * Bs > (long long)smemInts)
+                break;
+            capM = Ms;
+            capB = Bs;
+            mp = Ms;
+            if (Ms == n)
+                break;
+        }
+    }
+    int *S0 = smem, *S1 = S0 + capM, *sBkt = S1 + capM, *sNxt = sBkt + capM, *sRun = sNxt + capM;
+    int *sBmin = sRun + 2 * capM + 1, *sHead = sBmin + capB;
+    bool inS = capM > 0;
+    int *pos = inS ? S0 : w.posA, *npos = inS ? S1 : w.posB;
     int Mprev = 0;
     for (int stage = 0; stage < 64; ++stage) {
         const uint32_t B = hash_bucket_count((uint32_t)Mprev + 1);
         const int M = (uint32_t)n < B ? n : (int)B;
-        for (uint32_t b = tid; b < B; b += T) {
-            w.firstOld[b] = INT_MAX;
-            w.createNew[b] = INT_MAX;
-            w.head[b] = -1;
+        if (inS && M > capM) {
+            // leave shared memory: the previous stage's positions move to the global buffers
+            for (int i = tid; i < Mprev; i += T)
+                w.posA[i] = pos[i];
+            __syncthreads();
+            inS = false;
+            pos = w.posA;
+            npos = w.posB;
         }
-        for (int i = tid; i < M + Mprev; i += T)
-            w.runSize[i] = 0;
-        __syncthreads();
-        for (int i = tid; i < M; i += T) {
-            const uint32_t b = keys[i] % B;
-            if (i < Mprev)
-                atomicMin(&w.firstOld[b], pos[i]);
-            else
-                atomicMin(&w.createNew[b], i);
-            w.nxt[i] = atomicExch(&w.head[b], i);
-        }
-        __syncthreads();
-        // runs: opened by this stage's inserts [0, M - Mprev), latest first; rebuilt [M, M + Mprev)
-        for (int i = tid; i < M; i += T) {
-            const uint32_t b = keys[i] % B;
-            const int fo = w.firstOld[b];
-            const int slot = fo != INT_MAX ? M + (Mprev - 1 - fo) : (M - 1 - w.createNew[b]);
-            w.slotOf[i] = slot;
-            atomicAdd(&w.runSize[slot], 1);
-        }
-        __syncthreads();
-        block_excl_scan(w.runSize, M + Mprev);
-        for (int i = tid; i < M; i += T) {
-            const uint32_t b = keys[i] % B;
-            const int gi = i < Mprev ? 1 : 0;
-            const int ki = gi ? (Mprev - 1 - pos[i]) : (M - 1 - i);
-            int within = 0;
-            for (int j = w.head[b]; j >= 0; j = w.nxt[j]) {
-                if (j == i)
-                    continue;
-                const int gj = j < Mprev ? 1 : 0;
-                const int kj = gj ? (Mprev - 1 - pos[j]) : (M - 1 - j);
-                within += (gj < gi || (gj == gi && kj < ki)) ? 1 : 0;
-            }
-            npos[i] = w.runSize[w.slotOf[i]] + within;
-        }
-        __syncthreads();
+        if (inS)
+            hash_stage(keys, M, Mprev, B, pos, npos, sBkt, sNxt, sRun, sBmin, sHead);
+        else
+            hash_stage(keys, M, Mprev, B, pos, npos, w.slotOf, w.nxt, w.runSize, w.bmin, w.head);
         int *t = pos;
         pos = npos;
         npos = t;
@@ -160,7 +212,6 @@ __device__ void hash_order_block(const uint32_t *keys, int n, int *out, HashScra
         if (M == n)
             break;
     }
-    __syncthreads();
     for (int i = tid; i < n; i += T)
         out[i] = pos[i];
     __syncthreads();
@@ -225,8 +276,9 @@ __global__ void k_face_keys(FaceOrderArgs a)
 }
 
 // one block per mesh: the faces in insertion order (sorted by key) -> iteration order of the context map
-__global__ void __launch_bounds__(kOrderThreads) k_face_ctx(FaceOrderArgs a)
+__global__ void __launch_bounds__(kOrderThreads) k_face_ctx(FaceOrderArgs a, int smemInts)
 {
+    extern __shared__ __align__(16) int dsm[];
     const int side = blockIdx.x;
     const int off = side ? a.FA : 0, n = side ? a.FB : a.FA;
     uint32_t *keys = a.insKeys + off;
@@ -235,7 +287,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_face_ctx(FaceOrderArgs a)
     __syncthreads();
     const HashScratch w = a.hs[side];
     // the result lands in slotOf, which the stages no longer need when it is written
-    hash_order_block(keys, n, w.slotOf, w);
+    hash_order_block(keys, n, w.slotOf, w, dsm, smemInts);
     // the positions must be a permutation of [0, n); should they not be, the faces keep index order (and the
     // overflow counter reports it) rather than index out of bounds later
     __shared__ int bad;
@@ -268,12 +320,20 @@ void launch_face_keys(const FaceOrderArgs &a, cudaStream_t s)
     SB_COUNT(k_face_keys)<<<(a.nFaces + 255) / 256, 256, 0, s>>>(a);
 }
 
+constexpr int kFaceCtxSmemBytes = 226 * 1024; // of the 227 KB a block may take, leaving room for static arrays
+
 void launch_face_ctx(const FaceOrderArgs &a, cudaStream_t s)
 {
     if (a.nFaces <= 0)
         return;
+    static std::once_flag once;
+    static cudaError_t attrErr = cudaSuccess;
+    std::call_once(once, [] {
+        attrErr = cudaFuncSetAttribute(k_face_ctx, cudaFuncAttributeMaxDynamicSharedMemorySize, kFaceCtxSmemBytes);
+    });
+    const int bytes = attrErr == cudaSuccess ? kFaceCtxSmemBytes : 0;
     KTime kt("k_face_order", s);
-    SB_COUNT(k_face_ctx)<<<2, kOrderThreads, 0, s>>>(a);
+    SB_COUNT(k_face_ctx)<<<2, kOrderThreads, bytes, s>>>(a, bytes / 4);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -307,62 +367,108 @@ void launch_rank_scan(const RankScanArgs &a, cudaStream_t s)
 // ---------------------------------------------------------------------------------------------------
 // loops (buildPolygonsFromEdges, src/solidboolean.cpp:124-165) and the seeds of the face groups (:167-200)
 // ---------------------------------------------------------------------------------------------------
-size_t loop_order_flag_ints(int slotDomain, int nNew) { return (size_t)std::max(slotDomain, nNew) + 1; }
 
-// directed loop edge d = 2 x + k (x's k-th neighbour) -> the next directed edge along the loop, -1 if none
-__device__ __forceinline__ int loop_succ(const int *nbr, const int *degree, int d)
+// diagnostic: device time at phase boundaries of the one-block kernels (thread 0, after a barrier)
+__device__ __forceinline__ void phase_stamp(unsigned long long *stamps, int k)
 {
-    const int x = d >> 1;
-    if (degree[x] != 2)
-        return -1;
-    const int v = nbr[d];
-    if (v < 0 || degree[v] != 2)
-        return -1;
-    const int j = nbr[2 * v] == x ? 0 : 1;
-    return 2 * v + (1 - j);
+    if (stamps && threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        stamps[k] = t;
+    }
 }
+
+constexpr int kRulerStride = 8;   // every 8th appended vertex id on a loop is a ruler
+constexpr int kOrphanProbe = 64;  // a vertex that meets no ruler within this many steps becomes one
+
+// Bump allocation of one block's work arrays: from dynamic shared memory while it lasts, else from the
+// global scratch (which is sized for every array, so its offsets do not depend on what fitted).
+struct Bump {
+    int *sm;
+    long long smLeft;
+    int *gl;
+    __device__ int *take(long long n)
+    {
+        n = (n + 3) & ~3ll; // 16-byte alignment for int2 / int4 views
+        int *p;
+        if (n <= smLeft) {
+            p = sm;
+            sm += n;
+            smLeft -= n;
+        } else {
+            p = gl;
+        }
+        gl += n;
+        return p;
+    }
+    // where take(n) would place n ints, without taking them (a temporary that later takes overwrite)
+    __device__ int *peek(long long n) const { return ((n + 3) & ~3ll) <= smLeft ? sm : gl; }
+};
+
+size_t loop_order_scratch_ints(int slotDomain, int nNew)
+{
+    const long long N = std::max(nNew, 1), W = 2 * N + 2;
+    auto r4 = [](long long n) { return (n + 3) & ~3ll; };
+    // phase 1: flag; phase 3 on: adjacency, iteration positions, ruler ids, ruler vertices, 15 arrays per walk,
+    // the loop flag, 4 per loop
+    return (size_t)(r4(std::max<long long>(slotDomain, N) + 1) + r4(2 * N) + 3 * r4(N) + 15 * r4(W) + r4(N + 1) +
+                    4 * r4(N + 1) + 64);
+}
+
+__device__ __forceinline__ int other_nb(int2 nb, int prev) { return nb.x == prev ? nb.y : nb.x; }
 
 // One block. Loop vertices are the appended vertices on the first mesh's cut edges; every one has exactly two
 // neighbours (else combine fails and nothing here runs). In the loop map a vertex is inserted as a key at its
 // first occurrence in the edge sequence; the map's iteration order makes the loop list: each loop starts at
 // its vertex met first in that order and goes on to the neighbour its set iterates first, which for a set of
-// two is the one inserted second.
+// two is the one inserted second. Positions along the loops come from ruler walks: rulers (every 8th vertex
+// id, and one vertex of each loop that has none) walk both ways to the next ruler in shared memory, then
+// pointer jumping over the walks finds each loop's first vertex and ranks the walks from it.
 __global__ void __launch_bounds__(kOrderThreads) k_loop_order(LoopOrderArgs a)
 {
+    extern __shared__ __align__(16) int dsm[];
     const int T = blockDim.x, tid = threadIdx.x;
     if (*a.loopBad != 0 || a.nNew <= 0) {
         if (tid == 0)
             a.info[0] = a.info[1] = 0;
         return;
     }
-    const int nNew = a.nNew, nD = 2 * nNew;
+    const int nNew = a.nNew;
+    __shared__ int bad;
+    phase_stamp(a.stamps, 0);
     // 1. insertion sequence of the map's keys
+    int *flag;
+    {
+        Bump b1{dsm, a.smemInts, a.scratch};
+        flag = b1.take(max(a.slotDomain, nNew) + 1);
+    }
     for (int i = tid; i < a.slotDomain; i += T)
-        a.flag[i] = 0;
+        flag[i] = 0;
     __syncthreads();
     for (int x = tid; x < nNew; x += T)
-        if (a.degree[x] > 0)
-            a.flag[a.firstOcc[x]] = 1;
+        if (a.degree[x] > 0 && a.firstOcc[x] < a.slotDomain)
+            flag[a.firstOcc[x]] = 1;
     __syncthreads();
-    const int nLV = block_excl_scan(a.flag, a.slotDomain);
+    const int nLV = block_excl_scan(flag, a.slotDomain);
     for (int x = tid; x < nNew; x += T)
-        if (a.degree[x] > 0) {
-            const int r = a.flag[a.firstOcc[x]];
+        if (a.degree[x] > 0 && a.firstOcc[x] < a.slotDomain) {
+            const int r = flag[a.firstOcc[x]];
             a.insRank[x] = r;
             a.insKeys[r] = a.newBase + (uint32_t)x;
         }
     __syncthreads();
+    phase_stamp(a.stamps, 1);
     // 2. iteration order (checked to be a permutation before anything is indexed by it)
-    hash_order_block(a.insKeys, nLV, a.hashOut, a.hs);
-    __shared__ int bad;
+    hash_order_block(a.insKeys, nLV, a.hashOut, a.hs, dsm, (int)a.smemInts);
+    int *chk = a.scratch; // the phase-1 flag's global twin is free now
     if (tid == 0)
         bad = 0;
     for (int i = tid; i < nLV; i += T)
-        a.flag[i] = 0;
+        chk[i] = 0;
     __syncthreads();
     for (int i = tid; i < nLV; i += T) {
         const int p = a.hashOut[i];
-        if (p < 0 || p >= nLV || atomicAdd(&a.flag[p], 1) != 0)
+        if (p < 0 || p >= nLV || atomicAdd(&chk[p], 1) != 0)
             bad = 1;
     }
     __syncthreads();
@@ -373,144 +479,346 @@ __global__ void __launch_bounds__(kOrderThreads) k_loop_order(LoopOrderArgs a)
         }
         return;
     }
+    phase_stamp(a.stamps, 2);
+    // 3. work arrays of the walks
+    Bump bm{dsm, a.smemInts, a.scratch};
+    int2 *NB = reinterpret_cast<int2 *>(bm.take(2ll * nNew));
+    int *IT = bm.take(nNew), *RI = bm.take(nNew), *RV = bm.take(nNew);
+    for (int x = tid; x < nNew; x += T) {
+        const bool lv = a.degree[x] == 2;
+        NB[x] = lv ? make_int2(a.nbr[2 * x], a.nbr[2 * x + 1]) : make_int2(-1, -1);
+        IT[x] = lv ? a.hashOut[a.insRank[x]] : INT_MAX;
+        RI[x] = (lv && x % kRulerStride == 0) ? 1 : 0;
+    }
+    __syncthreads();
+    // rulers: the regular ones, plus the smallest vertex id of a loop that holds none, plus any vertex that
+    // meets no ruler within the probe length
+    for (int x = tid; x < nNew; x += T) {
+        if (NB[x].x < 0 || RI[x])
+            continue;
+        int prev = x, cur = NB[x].x, mnId = x, steps = 0;
+        bool hit = false;
+        while (cur != x && steps < kOrphanProbe) {
+            if (RI[cur] == 1) {
+                hit = true;
+                break;
+            }
+            mnId = min(mnId, cur);
+            const int nx = other_nb(NB[cur], prev);
+            prev = cur;
+            cur = nx;
+            ++steps;
+        }
+        if (!hit && (cur != x || mnId == x))
+            RI[x] = 2; // (the probes test RI == 1 only, so this write does not disturb them)
+    }
+    __syncthreads();
+    // ruler ids: RI[x] for rulers, -1 else; RV[id] = its vertex. The scan runs in a temporary that the walk
+    // arrays take over afterwards.
+    int *scanTmp = bm.peek(nNew);
     for (int x = tid; x < nNew; x += T)
-        a.iterPos[x] = a.degree[x] > 0 ? a.hashOut[a.insRank[x]] : INT_MAX;
+        scanTmp[x] = RI[x] ? 1 : 0;
+    __syncthreads();
+    const int nR = block_excl_scan(scanTmp, nNew);
+    for (int x = tid; x < nNew; x += T) {
+        if (RI[x]) {
+            RI[x] = scanTmp[x];
+            RV[scanTmp[x]] = x;
+        } else {
+            RI[x] = -1;
+        }
+    }
+    __syncthreads();
+    const int nW = 2 * nR;
+    int *wSucc = bm.take(nW), *wLen = bm.take(nW), *wMin = bm.take(nW), *wArg = bm.take(nW);
+    int *cmA = bm.take(nW), *cmB = bm.take(nW), *caA = bm.take(nW), *caB = bm.take(nW);
+    int *sA = bm.take(nW), *sB = bm.take(nW), *dA = bm.take(nW), *dB = bm.take(nW);
+    int *wLoop = bm.take(nW), *wP = bm.take(nW), *wReach = bm.take(nW);
+    int *lflag = bm.take(nLV + 1);
+    phase_stamp(a.stamps, 3);
+    // 4. the walks: walk w = 2 r + s leaves ruler RV[r] through its neighbour s and stops at the next ruler;
+    // vertex x passed from its neighbour e records (w, offset) in vis[2 x + e]
+    for (int w = tid; w < nW; w += T) {
+        const int r0 = RV[w >> 1];
+        int prev = r0, cur = (w & 1) ? NB[r0].y : NB[r0].x, off = 1, mn = IT[r0], arg = r0;
+        for (int steps = 0; steps <= nLV && RI[cur] < 0; ++steps) {
+            const int e = NB[cur].x == prev ? 0 : 1;
+            a.vis[2 * cur + e] = make_int2(w, off);
+            if (IT[cur] < mn) {
+                mn = IT[cur];
+                arg = cur;
+            }
+            const int nx = e == 0 ? NB[cur].y : NB[cur].x;
+            prev = cur;
+            cur = nx;
+            ++off;
+        }
+        const int j = NB[cur].x == prev ? 0 : 1;
+        wSucc[w] = RI[cur] >= 0 ? 2 * RI[cur] + (1 - j) : w;
+        wLen[w] = off;
+        wMin[w] = mn;
+        wArg[w] = arg;
+    }
     __syncthreads();
     int rounds = 1;
-    while ((1 << rounds) < nLV + 1)
+    while ((1 << rounds) < nW + 1)
         ++rounds;
     ++rounds;
-    // 3. smallest iteration position on each loop (pointer jumping over the directed edges)
-    for (int d = tid; d < nD; d += T) {
-        a.succA[d] = loop_succ(a.nbr, a.degree, d);
-        a.valA[d] = a.iterPos[d >> 1];
+    phase_stamp(a.stamps, 4);
+    // 5. each loop's first vertex in iteration order: pointer jumping (min) over the walks of one orientation
+    for (int w = tid; w < nW; w += T) {
+        sA[w] = wSucc[w];
+        cmA[w] = wMin[w];
+        caA[w] = wArg[w];
     }
     __syncthreads();
-    int *sA = a.succA, *sB = a.succB, *vA = a.valA, *vB = a.valB;
     for (int r = 0; r < rounds; ++r) {
-        for (int d = tid; d < nD; d += T) {
-            const int s = sA[d];
-            vB[d] = s >= 0 ? min(vA[d], vA[s]) : vA[d];
-            sB[d] = s >= 0 ? sA[s] : -1;
+        for (int w = tid; w < nW; w += T) {
+            const int sc = sA[w];
+            const bool take = cmA[sc] < cmA[w];
+            cmB[w] = take ? cmA[sc] : cmA[w];
+            caB[w] = take ? caA[sc] : caA[w];
+            sB[w] = sA[sc];
         }
         __syncthreads();
         int *t = sA;
         sA = sB;
         sB = t;
-        t = vA;
-        vA = vB;
-        vB = t;
+        t = cmA;
+        cmA = cmB;
+        cmB = t;
+        t = caA;
+        caA = caB;
+        caB = t;
     }
-    for (int d = tid; d < nD; d += T)
-        a.cyc[d] = vA[d];
-    // 4. loop starts in iteration order, the start edges, and the edge that closes each loop
+    // loops in iteration order of their first vertices
     for (int i = tid; i <= nLV; i += T)
-        a.flag[i] = 0;
+        lflag[i] = 0;
     __syncthreads();
-    for (int x = tid; x < nNew; x += T)
-        if (a.degree[x] == 2 && a.iterPos[x] == a.cyc[2 * x])
-            a.flag[a.iterPos[x]] = 1;
+    for (int w = tid; w < nW; w += T)
+        if (cmA[w] >= 0 && cmA[w] < nLV)
+            lflag[cmA[w]] = 1;
     __syncthreads();
-    const int nLoops = block_excl_scan(a.flag, nLV);
-    // ranking: distance of every directed edge to the closing edge of its loop's start orientation
-    for (int d = tid; d < nD; d += T) {
-        const int s = loop_succ(a.nbr, a.degree, d);
-        bool tail = false;
-        if (s >= 0) {
-            const int v = s >> 1;
-            if (a.iterPos[v] == a.cyc[2 * v]) {
-                const int ks = a.nbrSlot[2 * v] > a.nbrSlot[2 * v + 1] ? 0 : 1; // inserted later iterates first
-                tail = (s & 1) == ks;
+    const int nLoops = block_excl_scan(lflag, nLV);
+    int *lW0 = bm.take(nLoops + 1), *lO0 = bm.take(nLoops + 1), *lLen = bm.take(nLoops + 1);
+    int *lOff = bm.take(nLoops + 1);
+    for (int w = tid; w < nW; w += T) {
+        const int loop = lflag[cmA[w]];
+        wLoop[w] = loop;
+        // the walk holding the loop's first vertex s0 in the direction the loop takes (towards the neighbour
+        // inserted second), and s0's offset in it
+        const int s0 = caA[w];
+        const int ks = a.nbrSlot[2 * s0] > a.nbrSlot[2 * s0 + 1] ? 0 : 1;
+        const int toward = ks == 0 ? a.nbr[2 * s0] : a.nbr[2 * s0 + 1];
+        int W0, o0;
+        if (RI[s0] >= 0) {
+            W0 = 2 * RI[s0] + (NB[s0].x == toward ? 0 : 1);
+            o0 = 0;
+        } else {
+            const int e = NB[s0].x == toward ? 1 : 0; // entered from the other neighbour
+            const int2 rec = a.vis[2 * s0 + e];
+            W0 = rec.x;
+            o0 = rec.y;
+        }
+        if (W0 < 0 || W0 >= nW) { // cannot happen for loops of two-neighbour vertices; keep indices in range
+            W0 = w;
+            o0 = 0;
+            atomicAdd(a.loopErr, 1u);
+        }
+        lW0[loop] = W0; // every walk of the loop writes the same values
+        lO0[loop] = o0;
+    }
+    __syncthreads();
+    phase_stamp(a.stamps, 5);
+    // 6. rank the walks from the loop's first walk along its direction: cut the cycle before it, suffix sums
+    for (int w = tid; w < nW; w += T) {
+        const int sc = wSucc[w];
+        const bool tail = sc == lW0[wLoop[w]];
+        sA[w] = tail ? -1 : sc;
+        dA[w] = wLen[w];
+    }
+    __syncthreads();
+    for (int r = 0; r < rounds; ++r) {
+        for (int w = tid; w < nW; w += T) {
+            const int sc = sA[w];
+            dB[w] = sc >= 0 ? dA[w] + dA[sc] : dA[w];
+            sB[w] = sc >= 0 ? sA[sc] : -1;
+        }
+        __syncthreads();
+        int *t = sA;
+        sA = sB;
+        sB = t;
+        t = dA;
+        dA = dB;
+        dB = t;
+    }
+    for (int w = tid; w < nW; w += T)
+        wReach[w] = sA[w] == -1 ? 1 : 0;
+    __syncthreads();
+    for (int w = tid; w < nW; w += T) {
+        const int loop = wLoop[w];
+        const int L = dA[lW0[loop]];
+        wP[w] = L - dA[w]; // offset of the walk's first vertex after the first walk's first vertex
+        if (w == lW0[loop])
+            lLen[loop] = L;
+    }
+    __syncthreads();
+    for (int l = tid; l < nLoops; l += T)
+        lOff[l] = lLen[l];
+    __syncthreads();
+    block_excl_scan(lOff, nLoops);
+    phase_stamp(a.stamps, 6);
+    for (int i = tid; i < 2 * 2 * nLV; i += T)
+        a.seedTri[i] = -1;
+    for (int i = tid; i < nLV; i += T)
+        a.entryLoop[i] = -1;
+    __syncthreads();
+    // 7. every loop vertex's place: loop position p of loop l holds edge (l_p, l_p+1); entries 2 (off_l + p)
+    // and 2 (off_l + p) + 1 are its two half-edges (k_seed_entries looks their owners up, grid-wide)
+    for (int x = tid; x < nNew; x += T) {
+        int w = -1, o = 0, next = -1;
+        if (NB[x].x >= 0) {
+            if (RI[x] >= 0) {
+                for (int s2 = 0; s2 < 2; ++s2)
+                    if (wReach[2 * RI[x] + s2]) {
+                        w = 2 * RI[x] + s2;
+                        next = s2 ? NB[x].y : NB[x].x;
+                    }
+            } else {
+                for (int e = 0; e < 2; ++e) {
+                    const int2 rec = a.vis[2 * x + e];
+                    if (rec.x >= 0 && rec.x < nW && wReach[rec.x]) {
+                        w = rec.x;
+                        o = rec.y;
+                        next = e == 0 ? NB[x].y : NB[x].x;
+                    }
+                }
             }
         }
-        sA[d] = tail ? -1 : s;
-        vA[d] = (tail || s < 0) ? 0 : 1;
-    }
-    __syncthreads();
-    for (int r = 0; r < rounds; ++r) {
-        for (int d = tid; d < nD; d += T) {
-            const int s = sA[d];
-            vB[d] = s >= 0 ? vA[d] + vA[s] : vA[d];
-            sB[d] = s >= 0 ? sA[s] : -1;
+        int base = -1;
+        if (w >= 0) {
+            const int loop = wLoop[w], L = lLen[loop];
+            if (L > 0) {
+                int p = wP[w] + o - lO0[loop];
+                p = ((p % L) + L) % L;
+                base = lOff[loop] + p;
+                if (base < 0 || base >= nLV)
+                    base = -1;
+                else
+                    a.entryLoop[base] = loop;
+            }
         }
-        __syncthreads();
-        int *t = sA;
-        sA = sB;
-        sB = t;
-        t = vA;
-        vA = vB;
-        vB = t;
-    }
-    // loop lengths (at each start edge: distance + 1), then loop offsets
-    for (int x = tid; x < nNew; x += T)
-        if (a.degree[x] == 2 && a.iterPos[x] == a.cyc[2 * x]) {
-            const int ks = a.nbrSlot[2 * x] > a.nbrSlot[2 * x + 1] ? 0 : 1;
-            a.loopLen[a.flag[a.iterPos[x]]] = vA[2 * x + ks] + 1;
-        }
-    __syncthreads();
-    block_excl_scan(a.loopLen, nLoops);
-    // 5. seed entries: loop position p of loop l holds edge (l_p, l_p+1); its two half-edges' owners in each
-    // mesh are entries 2 (off_l + p) and 2 (off_l + p) + 1
-    const int nE = 2 * nLV;
-    for (int d = tid; d < nD; d += T) {
-        if (sA[d] != -1 || a.degree[d >> 1] != 2)
-            continue;
-        const int s0 = loop_succ(a.nbr, a.degree, d);
-        if (s0 < 0)
-            continue;
-        const int loop = a.flag[a.cyc[d]];
-        const int end = loop + 1 < nLoops ? a.loopLen[loop + 1] : nLV;
-        const int L = end - a.loopLen[loop];
-        const int p = L - 1 - vA[d];
-        if (p < 0 || p >= L)
-            continue;
-        const int base = a.loopLen[loop] + p;
-        a.entryLoop[base] = loop;
-        const uint32_t u = a.newBase + (uint32_t)(d >> 1), v = a.newBase + (uint32_t)a.nbr[d];
-        for (int m = 0; m < 2; ++m) {
-            const uint64_t *hk = m ? a.heKeysB : a.heKeysA;
-            const int *hv = m ? a.heValsB : a.heValsA;
-            a.seedTri[m * nE + 2 * base] = u64map_find(hk, hv, a.heMask, he_key(u, v));
-            a.seedTri[m * nE + 2 * base + 1] = u64map_find(hk, hv, a.heMask, he_key(v, u));
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < 2 * nE; i += T) {
-        const int t = a.seedTri[i];
-        if (t >= 0)
-            atomicMin(&a.firstQ[t], i % nE);
-    }
-    for (int i = tid; i < 2 * 2 * nLoops; i += T) {
-        a.group0[i] = INT_MAX;
-        a.gQuery[i] = -1;
-    }
-    __syncthreads();
-    // 6. each group's first triangle: its first entry whose triangle no earlier entry claimed
-    for (int i = tid; i < 2 * nE; i += T) {
-        const int t = a.seedTri[i], q = i % nE, m = i / nE;
-        if (t >= 0 && a.firstQ[t] == q)
-            atomicMin(&a.group0[m * 2 * nLoops + 2 * a.entryLoop[q >> 1] + (q & 1)], q);
-    }
-    __syncthreads();
-    for (int i = tid; i < 2 * 2 * nLoops; i += T) {
-        const int q = a.group0[i];
-        if (q == INT_MAX)
-            continue;
-        const int m = i / (2 * nLoops);
-        const unsigned int k = atomicAdd(a.qCount, 1u);
-        a.qTri[k] = a.seedTri[m * nE + q];
-        a.gQuery[i] = (int)k;
+        a.entryBase[x] = base;
+        a.entryNext[x] = next;
     }
     if (tid == 0) {
         a.info[0] = nLV;
         a.info[1] = nLoops;
     }
+    phase_stamp(a.stamps, 7);
 }
 
-void launch_loop_order(const LoopOrderArgs &a, cudaStream_t s)
+// The seed entries' triangles (the owners of each loop edge's two half-edges in each mesh), and the first
+// entry of every triangle. Grid-wide: the hash-table probes are latency-bound.
+__global__ void k_seed_entries(LoopOrderArgs a)
 {
-    KTime kt("k_loop_order", s);
-    SB_COUNT(k_loop_order)<<<1, kOrderThreads, 0, s>>>(a);
+    const int nLV = a.info[0], nLoops = a.info[1], nE = 2 * nLV;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < 4 * nLoops) {
+        a.group0[x] = INT_MAX;
+        a.gQuery[x] = -1;
+    }
+    if (x >= a.nNew)
+        return;
+    const int base = a.entryBase[x];
+    if (base < 0 || base >= nLV)
+        return;
+    const uint32_t u = a.newBase + (uint32_t)x, v = a.newBase + (uint32_t)a.entryNext[x];
+    for (int m = 0; m < 2; ++m) {
+        const uint64_t *hk = m ? a.heKeysB : a.heKeysA;
+        const int *hv = m ? a.heValsB : a.heValsA;
+        const int t0 = u64map_find(hk, hv, a.heMask, he_key(u, v));
+        const int t1 = u64map_find(hk, hv, a.heMask, he_key(v, u));
+        a.seedTri[m * nE + 2 * base] = t0;
+        a.seedTri[m * nE + 2 * base + 1] = t1;
+        if (t0 >= 0 && t0 < a.nTri)
+            atomicMin(&a.firstQ[t0], 2 * base);
+        if (t1 >= 0 && t1 < a.nTri)
+            atomicMin(&a.firstQ[t1], 2 * base + 1);
+    }
+}
+
+// each group's first triangle: its first entry whose triangle no earlier entry claimed
+__global__ void k_seed_groups(LoopOrderArgs a)
+{
+    const int nLV = a.info[0], nLoops = a.info[1], nE = 2 * nLV;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * nE)
+        return;
+    const int t = a.seedTri[i], q = i % nE, m = i / nE;
+    if (t < 0 || t >= a.nTri || a.firstQ[t] != q)
+        return;
+    const int l = a.entryLoop[q >> 1];
+    if (l >= 0 && l < nLoops)
+        atomicMin(&a.group0[m * 2 * nLoops + 2 * l + (q & 1)], q);
+}
+
+// The side queries: every non-empty group's first triangle, and every region without seeds (one of the
+// reference's remaining groups, src/solidboolean.cpp:231-238) by its smallest uncut triangle. Also counts the
+// regions per mesh.
+__global__ void k_side_queries(AsmArgs g, LoopOrderArgs a)
+{
+    const int nLV = a.info[0], nLoops = a.info[1], nE = 2 * nLV;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 4 * nLoops) {
+        const int q = a.group0[i];
+        if (q != INT_MAX) {
+            const int m = i / (2 * nLoops);
+            const unsigned int k = atomicAdd(a.qCount, 1u);
+            a.qTri[k] = a.seedTri[m * nE + q];
+            a.gQuery[i] = (int)k;
+        }
+    }
+    if (i >= g.nTri || g.parent[i] != i)
+        return;
+    g.repOfRoot[i] = -1;
+    if (g.seedMin[i] != INT_MAX) {
+        atomicAdd(g.counters + kCntRegionsA + g.triMesh[i], 1u);
+        return;
+    }
+    if (g.remMin[i] != INT_MAX) {
+        const unsigned int k = atomicAdd(a.qCount, 1u);
+        a.qTri[k] = g.remMin[i];
+        g.repOfRoot[i] = (int)k;
+        atomicAdd(g.counters + kCntRegionsA + g.triMesh[i], 1u);
+    }
+}
+
+constexpr int kOrderSmemBytes = 226 * 1024; // of the 227 KB a block may take, leaving room for static arrays
+
+void launch_loop_order(LoopOrderArgs a, cudaStream_t s)
+{
+    static std::once_flag once;
+    static cudaError_t attrErr = cudaSuccess;
+    std::call_once(once, [] {
+        attrErr = cudaFuncSetAttribute(k_loop_order, cudaFuncAttributeMaxDynamicSharedMemorySize, kOrderSmemBytes);
+    });
+    a.smemInts = attrErr == cudaSuccess ? kOrderSmemBytes / 4 : 0;
+    {
+        KTime kt("k_loop_order", s);
+        SB_COUNT(k_loop_order)<<<1, kOrderThreads, attrErr == cudaSuccess ? kOrderSmemBytes : 0, s>>>(a);
+    }
+    const int n = std::max(a.nNew, 1);
+    KTime kt("k_seed_entries", s);
+    SB_COUNT(k_seed_entries)<<<(n + 255) / 256, 256, 0, s>>>(a);
+    SB_COUNT(k_seed_groups)<<<(4 * n + 255) / 256, 256, 0, s>>>(a);
+}
+
+void launch_side_queries(const AsmArgs &g, const LoopOrderArgs &a, cudaStream_t s)
+{
+    const int n = std::max(g.nTri, 4 * std::max(a.nNew, 1));
+    KTime kt("k_side_queries", s);
+    SB_COUNT(k_side_queries)<<<(n + 255) / 256, 256, 0, s>>>(g, a);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -526,9 +834,12 @@ __device__ __forceinline__ bool entry_live(const FloodArgs &f, int i, int nE, in
 {
     t = f.seedTri[i];
     const int q = i % nE;
-    if (t < 0 || f.firstQ[t] != q)
+    if (t < 0 || t >= f.nTri || f.firstQ[t] != q)
         return false;
-    group = 2 * f.entryLoop[q >> 1] + (q & 1);
+    const int l = f.entryLoop[q >> 1];
+    if (l < 0 || l >= f.info[1])
+        return false;
+    group = 2 * l + (q & 1);
     return true;
 }
 
@@ -566,12 +877,16 @@ __global__ void __launch_bounds__(kOrderThreads) k_flood(AsmArgs g, FloodArgs f)
     __shared__ int nFront;
     // level 0: live entries of mixed regions, ordered by entry (both meshes interleaved: they never meet)
     const int nI = 2 * nE;
+    int any = 0;
     for (int i = tid; i < nI; i += T) {
         const int m = i & 1, q = i >> 1;
         int t, grp;
-        f.flag[i] = (entry_live(f, m * nE + q, nE, t, grp) && mixed_region(f, f.root[t])) ? 1 : 0;
+        const int on = (entry_live(f, m * nE + q, nE, t, grp) && mixed_region(f, f.root[t])) ? 1 : 0;
+        f.flag[i] = on;
+        any |= on;
     }
-    __syncthreads();
+    if (!__syncthreads_or(any))
+        return; // every region's groups agree: nothing to flood
     const int n0 = block_excl_scan(f.flag, nI);
     for (int i = tid; i < nI; i += T) {
         const int m = i & 1, q = i >> 1;

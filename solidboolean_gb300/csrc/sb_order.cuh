@@ -16,11 +16,11 @@
 
 namespace sbg {
 
-// Scratch of one hash-order problem of n keys (hash_order_block): 4 n + 2 n + 1 ints, plus 3 bucket arrays of
-// hash_bucket_count(n) ints.
+// Scratch of one hash-order problem of n keys (hash_order_block) for the stages that do not fit in shared
+// memory: 4 n + 2 n + 1 ints, plus 2 bucket arrays of hash_bucket_count(n) ints.
 struct HashScratch {
     int *posA, *posB, *slotOf, *nxt, *runSize;
-    int *firstOld, *createNew, *head;
+    int *bmin, *head;
 };
 size_t hash_scratch_ints(int n);
 HashScratch hash_scratch_at(int *base, int n);
@@ -57,9 +57,9 @@ struct RankScanArgs {
 };
 void launch_rank_scan(const RankScanArgs &a, cudaStream_t s);
 
-// Loops, seeds and group representatives (k_loop_order, one block).
+// Loops, seeds and group representatives (k_loop_order, one block, then grid-wide seed kernels).
 struct LoopOrderArgs {
-    int nNew;
+    int nNew, nTri;
     uint32_t newBase;
     int slotDomain; // every first occurrence lies below it
     const int *degree, *nbr, *nbrSlot, *firstOcc;
@@ -74,16 +74,24 @@ struct LoopOrderArgs {
     int *firstQ;    // [nTri] first seed entry of each triangle (INT_MAX: none), filled in by the kernel
     int *group0;    // [2][2 nNew] first live entry of each group (INT_MAX: empty)
     int *gQuery;    // [2][2 nNew] side query of each group (-1: none)
+    int *entryBase, *entryNext; // [nNew] per loop vertex: its loop position in the entry sequence, the next vertex
     int *qTri;      // side queries: their triangles
     unsigned int *qCount;
     int *info;      // [2] loop vertices, loops
     // scratch
-    int *flag, *insRank, *iterPos, *succA, *succB, *valA, *valB, *cyc, *loopLen, *hashOut;
-    uint32_t *insKeys;
-    HashScratch hs;
+    int *insRank, *hashOut;   // [nNew]
+    uint32_t *insKeys;        // [nNew]
+    int2 *vis;                // [2 nNew]
+    HashScratch hs;           // for n = nNew
+    int *scratch;             // loop_order_scratch_ints(): what does not fit in shared memory
+    long long smemInts;       // set by launch_loop_order
+    unsigned long long *stamps; // [8] device time at the phase boundaries (diagnostics; may be null)
 };
-size_t loop_order_flag_ints(int slotDomain, int nNew);
-void launch_loop_order(const LoopOrderArgs &a, cudaStream_t s);
+size_t loop_order_scratch_ints(int slotDomain, int nNew);
+// the loop order (one block), the seed entries and each group's first entry (grid-wide)
+void launch_loop_order(LoopOrderArgs a, cudaStream_t s);
+// side queries of the groups and of the regions without seeds (needs the union-find regions)
+void launch_side_queries(const AsmArgs &g, const LoopOrderArgs &a, cudaStream_t s);
 
 // Side of each region from its groups, then the exact first-in-first-out flood of the regions whose groups
 // were decided differently, then the per-triangle labels.

@@ -1,7 +1,8 @@
 """Generates the golden fixtures from the reference itself (oracle/_ref, compiled from the reference
 sources by oracle/Makefile). Run here, where the reference sources exist:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py             # small fixtures with full arrays, earcut fixtures
+    python tests/golden/make_golden.py --headline  # digests of the benchmark-sized workloads
 
 Each fixture stores the input meshes (so no generator drift can hide a change) and the reference's dumps.
 """
@@ -42,9 +43,40 @@ def cases():
         yield f"batch_pair_{key}", m, 100000
 
 
+def headline_cases():
+    """The benchmark-sized workloads, pinned by digests (their full arrays are tens of megabytes)."""
+    yield "pair_large_L7_weld1e8", lambda: mg.pair_large(1234, 7), 100000000
+    yield "pair_large_L7_weld1e5", lambda: mg.pair_large(1234, 7), 100000
+    yield "near_tangent_L6", lambda: mg.near_tangent(1234, 6), 100000
+
+    def dv():
+        va, fa, vb, fb, off = mg.diff_volume(1234, 5)
+        return va, fa, vb + off, fb
+    yield "diff_volume_L5_offsets", dv, 100000
+    yield "diff_volume_L5_offsets_weld1e8", dv, 100000000
+
+
+def make_headline(ref):
+    import json
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from parity import digests, input_digest
+    table = {}
+    for name, gen, q in headline_cases():
+        va, fa, vb, fb = gen()
+        d = ref.run(va, fa, vb, fb, q)
+        table[name] = {"quantum": q, "inputs": input_digest(va, fa, vb, fb), "candidates_count": len(d["cand"]),
+                       "triangles_count": len(d["newt"]), **digests(d, len(va) + len(vb), q)}
+        print(name, "status", d["status"], "candidates", len(d["cand"]), "triangles", len(d["newt"]))
+    with open(os.path.join(HERE, "headline_digests.json"), "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+
+
 def main():
     ref = oracle.reference()
     assert ref is not None, "the reference sources are needed to generate golden fixtures"
+    if "--headline" in sys.argv:
+        make_headline(ref)
+        return
     for name, (va, fa, vb, fb), q in cases():
         d = ref.run(va, fa, vb, fb, q)
         out = {k: d[k] for k in KEEP}

@@ -151,3 +151,42 @@ def max_coord_error(oracle: dict, gpu: dict, n_orig: int, factor: int) -> float:
         return 0.0
     err = np.abs(vo - vg) / np.maximum(np.abs(vo), 1e-300)
     return float(np.where(vo == vg, 0.0, err).max())
+
+
+def _sha(a) -> str:
+    import hashlib
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.dtype.str.encode() + str(a.shape).encode() + a.tobytes()).hexdigest()
+
+
+def input_digest(va, fa, vb, fb) -> str:
+    return _sha(np.concatenate([np.asarray(va, np.float64).ravel(), np.asarray(vb, np.float64).ravel()])) + \
+        _sha(np.concatenate([np.asarray(fa, np.int64).ravel(), np.asarray(fb, np.int64).ravel()]))[:16]
+
+
+def digests(d: dict, n_orig: int, factor: int) -> dict:
+    """SHA-256 digests of a boolean's stage arrays, from an oracle dump or a GPU result (run_boolean):
+    candidate pairs (sorted), intersecting pairs and their segments (sorted by pair), and for a successful
+    combine the result vertices and arrangement triangles in the reference's own order, every triangle's
+    label, and the three fetch results after canonical ordering."""
+    gpu = "isect_pairs" in d
+    out = {"status": int(d["status"])}
+    out["candidates"] = _sha(sorted_pairs(d["cand"]))
+    if gpu:
+        ip, sg = np.asarray(d["isect_pairs"]).reshape(-1, 2), np.asarray(d["isect_segs"]).reshape(-1, 6)
+    else:
+        hit = np.asarray(d["isect"]).astype(bool)
+        ip, sg = np.asarray(d["cand"]).reshape(-1, 2)[hit], np.asarray(d["seg"]).reshape(-1, 6)[hit]
+    o = np.lexsort((ip[:, 1], ip[:, 0]))
+    out["intersecting_pairs"] = _sha(ip[o].astype(np.int64))
+    out["segments"] = _sha(sg[o].astype(np.float64))
+    if out["status"] != 1:
+        return out
+    out["vertices"] = _sha(np.asarray(d["newv"], np.float64).reshape(-1, 3))
+    out["arrangement"] = _sha(np.asarray(d["newt"], np.int64).reshape(-1, 3))
+    labels = np.asarray(d["labels"], np.int64) if gpu else oracle_labels(d)
+    out["labels"] = _sha(labels.astype(np.int64))
+    remap, _ = canonical_ids(d["newv"], n_orig, factor)
+    for op in ("union", "diff", "intersect"):
+        out[op] = _sha(canonical_tris(d[op], remap))
+    return out

@@ -57,3 +57,18 @@ def test_batch_sample(gpu_lib, port, precision):
         va, fa, vb, fb, _ = mg.batch_pair(rng, 5)
         ref, got = _check(port, va, fa, vb, fb, 100000, precision)
         fails += ref["status"] == 0
+
+
+@pytest.mark.parametrize("name", ["pair_large_L7_weld1e8", "pair_large_L7_weld1e5", "near_tangent_L6",
+                                  "diff_volume_L5_offsets", "diff_volume_L5_offsets_weld1e8"])
+def test_headline_reference_digests(gpu_lib, name):
+    """The CUDA path against digests of the compiled reference's own arrays (not only against the port):
+    candidate and intersecting pairs, segments, and for a successful combine the result vertices and the
+    arrangement in the reference's order, the labels and the three results."""
+    from test_golden_headline import META, headline_inputs, load_table
+    from parity import digests, input_digest
+    want = load_table()[name]
+    va, fa, vb, fb = headline_inputs(name)
+    assert input_digest(va, fa, vb, fb) == want["inputs"]
+    got = sbg.run_boolean(va, fa, vb, fb, want["quantum"])
+    assert digests(got, len(va) + len(vb), want["quantum"]) == {k: v for k, v in want.items() if k not in META}
