@@ -126,8 +126,9 @@ sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t 
  * group), "tri_mesh" (int8 per arrangement triangle: 0 first mesh, 1 second), "new_sources" (int32 per
  * appended result vertex: 2 x its intersecting pair + the end of that pair's segment it was built from),
  * "rank_first" / "rank_second" (int32 per triangle: position in the reference tree's leaf order),
- * "loop_order_ns" (8 uint64: device time stamps at the phase boundaries of the loop-order stage, a
- * diagnostic). *bytes receives the size; out may be NULL. */
+ * "loop_order_ns" (8 uint64: device time stamps at the phase boundaries of the loop-order stage),
+ * "leaf_order_ns_first" / "_second" (96 uint64: per large-node level of the leaf-order build, the device
+ * time at its start, after its classification and after its split; zero past the last level) (diagnostics). *bytes receives the size; out may be NULL. */
 sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
 void sb_boolean_destroy(sb_boolean *b);
 

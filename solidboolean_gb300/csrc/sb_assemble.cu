@@ -871,7 +871,7 @@ void launch_loops(const AsmArgs &g, cudaStream_t s)
         }
 }
 
-void launch_groups(const AsmArgs &g, cudaStream_t s)
+void launch_halfedges(const AsmArgs &g, cudaStream_t s)
 {
     if (g.nTri <= 0)
         return;
@@ -883,6 +883,19 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
                                                                        g.heKeysA, g.heValsA, g.heKeysB, g.heValsB,
                                                                        g.heMask);
         }
+    } else {
+        KTime kt("k_halfedges", s);
+        SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA,
+                                                             g.heKeysB, g.heValsB, g.heMask, g.uncutA + g.uncutB,
+                                                             g.origUncut, g.truncOcc);
+    }
+}
+
+void launch_groups(const AsmArgs &g, cudaStream_t s)
+{
+    if (g.nTri <= 0)
+        return;
+    if (g.useAdj) {
         KTime kt("k_union", s);
         SB_COUNT(k_union_adj)<<<nb(g.nTri, 256), 256, 0, s>>>(
             g.nTri, g.uncutA, g.uncutB, g.newT, g.triMesh, g.origUncut, g.retriFace, g.faceTri, g.A, g.B, g.cutA,
@@ -890,12 +903,6 @@ void launch_groups(const AsmArgs &g, cudaStream_t s)
             g.edgeVals, g.edgeMask,
             (uint32_t)g.newBase, g.parent, g.seedFlag, g.counters + kCntDupHalfedge);
     } else {
-        {
-            KTime kt("k_halfedges", s);
-            SB_COUNT(k_halfedges)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA,
-                                                                 g.heKeysB, g.heValsB, g.heMask,
-                                                                 g.uncutA + g.uncutB, g.origUncut, g.truncOcc);
-        }
         KTime kt("k_union", s);
         SB_COUNT(k_union)<<<nb(g.nTri, 256), 256, 0, s>>>(g.nTri, g.newT, g.triMesh, g.heKeysA, g.heValsA, g.heKeysB,
                                                          g.heValsB, g.heMask, g.edgeKeys, g.edgeVals, g.edgeMask,

@@ -140,6 +140,9 @@ void launch_weld_number(const AsmArgs &g, int nSeq, cudaStream_t s);
 void launch_mark_cut(const AsmArgs &g, cudaStream_t s);
 void launch_arrangement(const AsmArgs &g, cudaStream_t s);
 void launch_loops(const AsmArgs &g, cudaStream_t s);
+// the per-mesh half-edge tables (owners of directed edges)
+void launch_halfedges(const AsmArgs &g, cudaStream_t s);
+// union-find regions over the arrangement (after launch_halfedges), each region's seed and uncut minima
 void launch_groups(const AsmArgs &g, cudaStream_t s);
 void launch_sides(const AsmArgs &g, unsigned int nQueries, bool fp64, cudaStream_t s);
 // layout of the side-ray buffers for nRays rays (base null: bytes only)

@@ -721,6 +721,13 @@ sb_status combine_impl(sb_boolean *b)
             SB_CUDA_CHECK(cudaEventCreate(&e));
         b->evInit = true;
     }
+    // the second stream (work that runs beside the main chain) and its hand-over events
+    if (!b->side) {
+        SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+        SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->sideDone, cudaEventDisableTiming));
+    }
+    if (!b->orderDone)
+        SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->orderDone, cudaEventDisableTiming));
     // the meshes may have been prepared on other streams
     for (const sb_mesh *cm : {b->first, b->second})
         if (cm->readyEv)
@@ -1014,12 +1021,6 @@ sb_status combine_impl(sb_boolean *b)
         totals[2] = tTot;
         totals[3] = eTot;
         // the processing order runs on the second stream beside the re-triangulation (the weld waits for it)
-        if (!b->side) {
-            SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
-            SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->sideDone, cudaEventDisableTiming));
-        }
-        if (!b->orderDone)
-            SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->orderDone, cudaEventDisableTiming));
         cudaStream_t so = b->side;
         SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
         SB_CUDA_CHECK(cudaStreamWaitEvent(so, b->sideDone, 0));
@@ -1324,7 +1325,7 @@ sb_status combine_impl(sb_boolean *b)
         fl.launch();
     }
     launch_loops(g, s);
-    launch_groups(g, s);
+    launch_halfedges(g, s);
     // the loops in the reference's order, the group seeds and each group's first triangle
     const size_t nNewS = (size_t)std::max(nNew, 1), nTriS = (size_t)std::max(nTri, 1);
     const int slotDomain = 4 * (int)K; // first-mesh faces hold 2 K directed cut-edge slots, two sequence slots each
@@ -1405,7 +1406,14 @@ sb_status combine_impl(sb_boolean *b)
         fl.i32(fd.best, nTriS, INT_MAX);
         fl.launch();
     }
-    launch_loop_order(lo, s);
+    // the loop order needs the loop and half-edge tables only: it runs on the second stream beside the
+    // union-find regions, which the side queries need as well
+    SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
+    SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
+    launch_loop_order(lo, b->side);
+    SB_CUDA_CHECK(cudaEventRecord(b->orderDone, b->side));
+    launch_groups(g, s);
+    SB_CUDA_CHECK(cudaStreamWaitEvent(s, b->orderDone, 0));
     launch_side_queries(g, lo, s);
     SB_CUDA_CHECK(cudaGetLastError());
     SB_CUDA_CHECK(cudaEventRecord(b->ev[5], s));
@@ -1901,6 +1909,11 @@ sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_b
         // device time stamps (ns) at the phase boundaries of the loop-order kernel of the last combine
         sz = sizeof(unsigned long long) * 8;
         src = b->small.as<char>() + 1024;
+    } else if (n == "leaf_order_ns_first" || n == "leaf_order_ns_second") {
+        // device time stamps (ns) of the leaf-order build's large-node levels: start, classified, split
+        const MeshDev &M = n == "leaf_order_ns_first" ? b->first->d : b->second->d;
+        sz = M.levelStamps ? sizeof(unsigned long long) * 96 : 0;
+        src = M.levelStamps;
     } else if (n == "rank_first" || n == "rank_second") {
         const MeshDev &M = n == "rank_first" ? b->first->d : b->second->d;
         sz = M.rankValid ? sizeof(int) * (size_t)M.nt : 0;

@@ -55,6 +55,7 @@ struct MeshDev {
     // left + 1), -1 for a leaf}; node 0 is the root. Valid with rank.
     int4 *tnode = nullptr;
     int tnodeCount = 0;       // records the node table holds
+    unsigned long long *levelStamps = nullptr; // [96] diagnostic: device time per large-node level (3 each)
     bool rankValid = false;
     // [nt*3] for edge k of triangle i (t[k] -> t[k+1]): the first triangle in index order holding the reverse
     // edge, -1 for none. Depends on the triangles only, so a vertex update keeps it.

@@ -240,6 +240,31 @@ __device__ __forceinline__ bool warp_segment_reduce(int key, EStat &r, int &len)
     return lane == 31 || nextKey != key;
 }
 
+// Reduction of a whole warp whose 32 lanes share one key, with the warp reduction instructions on 32-bit
+// words: a 64-bit minimum is the minimum high word, then the minimum low word among the lanes holding it (the
+// maximum likewise); a fixed-point sum is summed as its signed high word and two 16-bit pieces of its low word
+// (each member's |sum| is below 2^(62 - bits(nt)) with nt > 1024, so every partial sum fits its 32 bits). All
+// lanes receive the totals. All 32 lanes must call it.
+__device__ __forceinline__ void warp_uniform_reduce(EStat &e, int &len)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    for (int k = 0; k < 3; ++k) {
+        const unsigned lh = (unsigned)(e.lo[k] >> 32), hh = (unsigned)(e.hi[k] >> 32);
+        const unsigned mlh = __reduce_min_sync(full, lh), mhh = __reduce_max_sync(full, hh);
+        const unsigned mll = __reduce_min_sync(full, lh == mlh ? (unsigned)e.lo[k] : 0xFFFFFFFFu);
+        const unsigned mhl = __reduce_max_sync(full, hh == mhh ? (unsigned)e.hi[k] : 0u);
+        e.lo[k] = ((unsigned long long)mlh << 32) | mll;
+        e.hi[k] = ((unsigned long long)mhh << 32) | mhl;
+        const unsigned long long u = (unsigned long long)e.s[k];
+        const int sh = __reduce_add_sync(full, (int)(unsigned)(u >> 32));
+        const unsigned s1 = __reduce_add_sync(full, (unsigned)(u >> 16) & 0xFFFFu);
+        const unsigned s0 = __reduce_add_sync(full, (unsigned)u & 0xFFFFu);
+        e.s[k] = (long long)(((unsigned long long)(long long)sh << 32) + ((unsigned long long)s1 << 16) +
+                             (unsigned long long)s0);
+    }
+    len = (int)__reduce_add_sync(full, (unsigned)len);
+}
+
 // Segmented inclusive scan over the 32 lanes: a lane with `start` set begins a new segment (lane 0 must).
 __device__ __forceinline__ void warp_segmented_scan(bool start, EStat &r)
 {
@@ -664,13 +689,16 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
     int openKey = -1, openLen = 0; // lane 0's carried run
     EStat open;
     estat_neutral(open);
+    // the state words of the next chunk are loaded while this one is processed
+    int vNext = wb + lane < we ? __ldcg(&state[wb + lane]) : 0;
     for (int base = wb; base < we; base += 32) {
         const int p = base + lane;
         int key = -1;
         EStat e;
         estat_neutral(e);
+        const int v = vNext;
+        vNext = base + 32 + lane < we ? __ldcg(&state[base + 32 + lane]) : 0;
         if (p < we) {
-            const int v = __ldcg(&state[p]);
             int node = st_node(v), tag = st_tag(v);
             if (tag == 1 || tag == 2) {
                 const int c = childTab && node >= prevFirst ? tab.child[node - prevFirst] : __ldcg(&np[node].child);
@@ -681,18 +709,21 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
             if (node >= first && node < last) {
                 const NParam q = parTab ? tab.par[node - first] : ld_nparam(&np[node]);
                 if (q.count > kSub) {
+                    // the split-axis key and the box and sum fields in one round trip (the fields go unused
+                    // for the rare member inside the interval)
                     const unsigned long long o = soa[(size_t)q.axis * nt + p];
+                    for (int k = 0; k < 3; ++k) {
+                        e.lo[k] = soa[(size_t)(3 + k) * nt + p];
+                        e.hi[k] = soa[(size_t)(6 + k) * nt + p];
+                        e.s[k] = (long long)soa[(size_t)(9 + k) * nt + p];
+                    }
                     const int sd = o < q.clo ? 0 : (o >= q.chi ? 1 : 2);
                     tag = sd + 1;
                     if (sd == 2) {
                         atomicOr(&nodes[node].flags, 1);
+                        estat_neutral(e);
                     } else {
                         key = (node - first) * 2 + sd;
-                        for (int k = 0; k < 3; ++k) {
-                            e.lo[k] = soa[(size_t)(3 + k) * nt + p];
-                            e.hi[k] = soa[(size_t)(6 + k) * nt + p];
-                            e.s[k] = (long long)soa[(size_t)(9 + k) * nt + p];
-                        }
                     }
                 }
             }
@@ -701,6 +732,26 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
                 state[p] = nv;
         }
         int len = key >= 0 ? 1 : 0;
+        // the usual case in Morton order: the whole chunk holds one key (or none). Its totals join the carried
+        // run when the key continues it, else the carried run is flushed and this chunk opens the next one;
+        // a chunk without keys leaves the carried run open (runs of one key merge in any grouping).
+        const int key0 = __shfl_sync(full, key, 0);
+        if (__all_sync(full, key == key0)) {
+            if (key0 < 0)
+                continue;
+            warp_uniform_reduce(e, len);
+            if (openKey == key0) {
+                estat_merge(open, e);
+                openLen += len;
+            } else {
+                if (openKey >= 0 && lane == 0)
+                    stat_atomic(target(openKey), open, openLen);
+                openKey = key0;
+                openLen = len;
+                open = e;
+            }
+            continue;
+        }
         // the carried run continues into lane 0 or is complete
         if (lane == 0) {
             if (openKey >= 0 && openKey == key) {
@@ -935,7 +986,8 @@ __device__ void create_children(int id, RNode *nodes, NParam *np, int *counters,
 __global__ void __launch_bounds__(kElemThreads, 4)
     k_rr_top(int nt, const RRec *__restrict__ rec, const unsigned long long *__restrict__ soa, int *state, NParam *np,
              RNode *nodes, int *counters, int *terms,
-             int maxNodes, const int *__restrict__ posOf, int *pool, const int *__restrict__ scg, GridBar *gb)
+             int maxNodes, const int *__restrict__ posOf, int *pool, const int *__restrict__ scg, GridBar *gb,
+             unsigned long long *stamps)
 {
     __shared__ RunRec runs[kRunCap];
     __shared__ int warpRuns[32];
@@ -945,7 +997,14 @@ __global__ void __launch_bounds__(kElemThreads, 4)
     const int sc[3] = {scg[0], scg[1], scg[2]};
     __shared__ LevelTab tab;
     int first = __ldcg(&counters[kCtFirst]), last = __ldcg(&counters[kCtLast]), prevFirst = first;
+    // diagnostic: block 0 stamps the device time at each level's start, after its classification and after
+    // its children (levels beyond the 32 recorded are not stamped)
+    auto stamp = [&](int level, int k) {
+        if (stamps && blockIdx.x == 0 && threadIdx.x == 0 && level < 32)
+            stamps[3 * level + k] = global_ns();
+    };
     for (int level = 0; level < kMaxLevels && first < last; ++level) {
+        stamp(level, 0);
         load_level_tab(tab, np, prevFirst, first, last);
         {
             // contiguous Morton ranges: block slices of whole chunks, split among the block's warps
@@ -960,6 +1019,7 @@ __global__ void __launch_bounds__(kElemThreads, 4)
         }
         if (!grid_sync(gb))
             return;
+        stamp(level, 1);
         for (int id = first + blockIdx.x; id < last; id += gridDim.x) {
             RNode &nd = nodes[id];
             const int count = __ldcg(&nd.count);
@@ -974,6 +1034,7 @@ __global__ void __launch_bounds__(kElemThreads, 4)
         }
         if (!grid_sync(gb))
             return;
+        stamp(level, 2);
         prevFirst = first;
         first = last;
         last = min(__ldcg(&counters[kCtNodes]), maxNodes);
@@ -1448,11 +1509,11 @@ static void coop_cancel(int dev, int blocks)
     g_coop.cv.notify_all();
 }
 
-// Blocks of the cooperative large-node kernel: a quarter of what can be resident at once, no more than the
+// Blocks of the cooperative large-node kernel: a third of what can be resident at once, no more than the
 // members need. The two meshes of a boolean build their leaf orders concurrently, and each grid holds its SMs'
-// whole register file until it ends: with a quarter each, half of the device stays free for the LBVH builds
-// and the broad and narrow phases that run meanwhile (measured on pair_large L7: the candidate search stage
-// 0.305 -> 0.165 ms, the boolean 2.01 -> 1.98 ms; an eighth makes the leaf order the longer path).
+// whole register file until it ends; the leaf order is the longer path, but the LBVH builds and the broad and
+// narrow phases run meanwhile on what is left (measured on pair_large L7, boolean step: a quarter each
+// 2.25 ms, a third 2.20 ms, a half 2.28 ms, where the candidate search is starved).
 static int top_grid(int nt, int *devOut)
 {
     static int perSm[256], sms[256];
@@ -1478,7 +1539,7 @@ static int top_grid(int nt, int *devOut)
     }
     *devOut = dev;
     const int need = (nt + kElemThreads * 4 - 1) / (kElemThreads * 4); // at least 4 members per thread
-    return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 4)));
+    return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 3)));
 }
 
 // Status of a leaf-order build from its counters and barrier record (12 ints).
@@ -1601,7 +1662,7 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
                  o_sc = c.take<int>(4), o_bar = c.take<GridBar>(1), o_cub = c.take<char>(sortBytes);
     // node table: the large nodes (ids below maxNodes) and at most 2 nt subtree nodes
     const int tnodeCap = maxNodes + 2 * nt + 2;
-    const size_t o_tn = c.take<int4>(tnodeCap);
+    const size_t o_tn = c.take<int4>(tnodeCap), o_stamp = c.take<unsigned long long>(96);
     SB_CUDA_CHECK(m->rankTmp.ensure(c.off));
     char *b = m->rankTmp.as<char>();
     RRec *rec = (RRec *)(b + o_rec);
@@ -1616,6 +1677,9 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     int4 *tnode = (int4 *)(b + o_tn);
     d.tnode = tnode;
     d.tnodeCount = tnodeCap;
+    unsigned long long *stamps = (unsigned long long *)(b + o_stamp);
+    d.levelStamps = stamps;
+    SB_CUDA_CHECK(cudaMemsetAsync(stamps, 0, 96 * sizeof(unsigned long long), s));
 
     const int GE = (nt + kElemThreads - 1) / kElemThreads;
     SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters, reinterpret_cast<unsigned *>(bar));
@@ -1634,7 +1698,8 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
             return SB_ERR_CUDA;
         SB_CUDA_CHECK(coop_acquire(dev, topBlocks));
         void *args[] = {(void *)&nt, (void *)&rec, (void *)&soa, (void *)&state, (void *)&np, (void *)&nodes, (void *)&counters,
-                        (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar};
+                        (void *)&terms, (void *)&maxNodes, (void *)&posOf, (void *)&pool, (void *)&scg, (void *)&bar,
+                        (void *)&stamps};
         count_launch();
         KTime kt("k_rr_top", s);
         const cudaError_t le =
