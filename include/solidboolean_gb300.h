@@ -132,6 +132,16 @@ sb_status sb_result_vertices_device(sb_boolean *b, const double **d_xyz, size_t 
 sb_status sb_debug_dump(sb_boolean *b, const char *name, void *out, size_t cap_bytes, size_t *bytes);
 void sb_boolean_destroy(sb_boolean *b);
 
+/* Diagnostic; its counterpart is mapbox::earcut (thirdparty/earcut.hpp/include/mapbox/earcut.hpp:833-838)
+ * as the reference's ReTriangulator calls it. Runs the device ear-clipper that sb_combine uses inside cut
+ * faces on one polygon with holes: xy [ring_off[n_rings] * 2] host doubles, rings back to back (the first
+ * is the outer ring), ring_off [n_rings + 1] CSR offsets. Writes the triangle vertex indices (into the
+ * concatenated rings, three per triangle) to indices (host, cap entries; NULL to query the count). Returns
+ * SB_ERR_CAPACITY when the device's fixed scratch or iteration budget for the polygon's size is exceeded.
+ * Allocates device memory and synchronises the device. */
+sb_status sb_debug_earcut(const double *xy, const int64_t *ring_off, size_t n_rings, int64_t *indices, size_t cap,
+                          size_t *count);
+
 /* No counterpart in the reference. Re-triangulates cut faces exactly as sb_combine does, for callers that
  * cannot allocate device memory: code inside a framework that owns all device memory through its own pool
  * (an allocation behind its back breaks its accounting and can fail once the pool holds the free memory),

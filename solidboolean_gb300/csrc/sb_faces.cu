@@ -16,6 +16,8 @@
 //   5. ear-clip every polygon with its holes and every inner loop with its children (:238-325).
 // The per-face scratch is carved from one device buffer at an offset given by a prefix sum of each face's
 // bound, so all faces run independently.
+#include <vector>
+
 #include "sb_common.cuh"
 #include "sb_earcut.cuh"
 #include "sb_faces.cuh"
@@ -663,4 +665,99 @@ void launch_faces(const FaceArgs &a, cudaStream_t s)
     SB_COUNT(k_faces)<<<(a.nFaces + kFacesPerWarp - 1) / kFacesPerWarp, 32, 0, s>>>(a);
 }
 
+// ---------------------------------------------------------------------------------------------------
+// The device ear-clipper on its own (sb_debug_earcut): one polygon with holes, one thread, with the same
+// scratch sizing rule as a cut face (nodes 6 L + 16, output 3 x nodes, stack 2 L + 8 for L ring points).
+// ---------------------------------------------------------------------------------------------------
+__global__ void k_earcut_one(const double *__restrict__ xy, const int *__restrict__ off, int nrings, int L,
+                             EcNode *nodes, int nodeCap, int *out, int outCap, int2 *stk, int stkCap, int *hq,
+                             int *ids, d2 *pts, int *result)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0)
+        return;
+    for (int i = 0; i < L; ++i) {
+        pts[i] = d2{xy[2 * i], xy[2 * i + 1]};
+        ids[i] = i;
+    }
+    DevEarcut ec;
+    ec.N = nodes;
+    ec.cap = nodeCap;
+    ec.out = out;
+    ec.outCap = outCap;
+    ec.stk = stk;
+    ec.stkCap = stkCap;
+    ec.hq = hq;
+    ec.error = 0;
+    ec.budget = 64ll * L * L + 100000;
+    ec.run(pts, ids, off, nrings);
+    result[0] = ec.outCnt;
+    result[1] = ec.error;
+}
+
 } // namespace sbg
+
+using namespace sbg;
+
+extern "C" sb_status sb_debug_earcut(const double *xy, const int64_t *ring_off, size_t n_rings, int64_t *indices,
+                                     size_t cap, size_t *count)
+{
+    if (!xy || !ring_off || !count || n_rings == 0 || n_rings > (1u << 20))
+        return SB_ERR_INVALID;
+    const int64_t L64 = ring_off[n_rings];
+    if (ring_off[0] != 0 || L64 <= 0 || L64 > (1 << 20))
+        return SB_ERR_INVALID;
+    for (size_t r = 0; r < n_rings; ++r)
+        if (ring_off[r + 1] < ring_off[r])
+            return SB_ERR_INVALID;
+    const int L = (int)L64;
+    const int nodeCap = 6 * L + 16, outCap = 3 * nodeCap, stkCap = 2 * L + 8;
+    std::vector<int> off(n_rings + 1);
+    for (size_t r = 0; r <= n_rings; ++r)
+        off[r] = (int)ring_off[r];
+    DevBuf buf;
+    Carve c;
+    const size_t o_xy = c.take<double>(2 * (size_t)L), o_off = c.take<int>(n_rings + 1);
+    const size_t o_nodes = c.take<EcNode>(nodeCap), o_out = c.take<int>(outCap), o_stk = c.take<int2>(stkCap);
+    const size_t o_hq = c.take<int>(n_rings + 1), o_ids = c.take<int>(L), o_pts = c.take<d2>(L);
+    const size_t o_res = c.take<int>(2);
+    SB_CUDA_CHECK(buf.ensure(c.off));
+    char *b = buf.as<char>();
+    sb_status st = SB_OK;
+    int res[2] = {0, 0};
+    std::vector<int> out;
+    cudaError_t e = cudaMemcpy(b + o_xy, xy, sizeof(double) * 2 * (size_t)L, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b + o_off, off.data(), sizeof(int) * (n_rings + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        count_launch();
+        k_earcut_one<<<1, 32>>>((const double *)(b + o_xy), (const int *)(b + o_off), (int)n_rings, L,
+                                (EcNode *)(b + o_nodes), nodeCap, (int *)(b + o_out), outCap, (int2 *)(b + o_stk),
+                                stkCap, (int *)(b + o_hq), (int *)(b + o_ids), (d2 *)(b + o_pts),
+                                (int *)(b + o_res));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(res, b + o_res, sizeof res, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && res[1] == 0 && res[0] > 0) {
+        out.resize((size_t)res[0]);
+        e = cudaMemcpy(out.data(), b + o_out, sizeof(int) * out.size(), cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "sb_debug_earcut", __FILE__, __LINE__);
+    } else if (res[1] != 0) {
+        set_last_error(res[1] == 1 ? "earcut: node capacity exceeded" : "earcut: iteration budget exceeded");
+        st = SB_ERR_CAPACITY;
+    } else {
+        *count = out.size();
+        if (indices) {
+            if (cap < out.size()) {
+                st = SB_ERR_INVALID;
+            } else {
+                for (size_t k = 0; k < out.size(); ++k)
+                    indices[k] = out[k];
+            }
+        }
+    }
+    buf.release();
+    return st;
+}

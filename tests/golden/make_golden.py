@@ -3,6 +3,7 @@ sources by oracle/Makefile). Run here, where the reference sources exist:
 
     python tests/golden/make_golden.py             # small fixtures with full arrays, earcut fixtures
     python tests/golden/make_golden.py --headline  # digests of the benchmark-sized workloads
+    python tests/golden/make_golden.py --cases     # the reference's test meshes and earcut fixtures
 
 Each fixture stores the input meshes (so no generator drift can hide a change) and the reference's dumps.
 """
@@ -71,11 +72,75 @@ def make_headline(ref):
         json.dump(table, f, indent=1, sort_keys=True)
 
 
+def earcut_fixture_polygons():
+    """The reference's earcut fixtures (thirdparty/earcut.hpp/test/fixtures/*.cpp), read from its test files."""
+    import glob
+    import re
+    root = os.path.join(oracle.REF_ROOT, "thirdparty", "earcut.hpp", "test", "fixtures")
+    for path in sorted(glob.glob(os.path.join(root, "*.cpp"))):
+        text = open(path).read()
+        m = re.search(r"Fixture<\w+>\s+\w+\(\"(\w+)\",\s*\d+,[^{]*\{(.*)\}\);", text, re.S)
+        if not m:
+            continue
+        rings = []
+        for ring in re.findall(r"\{((?:\{[-0-9.eE+]+,[-0-9.eE+]+\},?)+)\}", m.group(2)):
+            pts = re.findall(r"\{([-0-9.eE+]+),([-0-9.eE+]+)\}", ring)
+            rings.append(np.array([[float(x), float(y)] for x, y in pts]))
+        if rings:
+            yield m.group(1), rings
+
+
+def make_cases(ref):
+    """The reference's own test meshes (test/cases/*/{a,b}.obj, read like its test driver reads them) with
+    digests of the reference's results at both weld factors, and its earcut fixtures with the reference's
+    triangle indices."""
+    import glob
+    import json
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from parity import digests, input_digest
+    from solidboolean_gb300 import objio
+    arrays, table = {}, {}
+    root = os.path.join(oracle.REF_ROOT, "test", "cases")
+    for d in sorted(glob.glob(os.path.join(root, "*"))):
+        name = os.path.basename(d)
+        a, b = os.path.join(d, "a.obj"), os.path.join(d, "b.obj")
+        if not (os.path.isfile(a) and os.path.isfile(b)):
+            continue
+        va, fa = objio.load_obj(a)
+        vb, fb = objio.load_obj(b)
+        arrays.update({f"{name}:va": va, f"{name}:fa": fa, f"{name}:vb": vb, f"{name}:fb": fb})
+        for q in (100000, 100000000):
+            r = ref.run(va, fa, vb, fb, q)
+            table[f"{name}:{q}"] = {"inputs": input_digest(va, fa, vb, fb), "quantum": q,
+                                    **digests(r, len(va) + len(vb), q)}
+            print(name, q, "status", r["status"], "triangles", len(r["newt"]))
+    np.savez_compressed(os.path.join(HERE, "reference_meshes.npz"), **arrays)
+    with open(os.path.join(HERE, "reference_meshes_digests.json"), "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    xy, ring_off, poly_off, idx, idx_off, names = [], [0], [0], [], [0], []
+    for name, rings in earcut_fixture_polygons():
+        for r in rings:
+            xy.append(r)
+            ring_off.append(ring_off[-1] + len(r))
+        poly_off.append(poly_off[-1] + len(rings))
+        ix = ref.earcut(rings)
+        idx.append(ix)
+        idx_off.append(idx_off[-1] + len(ix))
+        names.append(name)
+    np.savez_compressed(os.path.join(HERE, "earcut_reference_fixtures.npz"), xy=np.concatenate(xy),
+                        ring_off=np.array(ring_off), poly_off=np.array(poly_off), idx=np.concatenate(idx),
+                        idx_off=np.array(idx_off), names=np.array(names))
+    print("earcut fixtures", len(names))
+
+
 def main():
     ref = oracle.reference()
     assert ref is not None, "the reference sources are needed to generate golden fixtures"
     if "--headline" in sys.argv:
         make_headline(ref)
+        return
+    if "--cases" in sys.argv:
+        make_cases(ref)
         return
     for name, (va, fa, vb, fb), q in cases():
         d = ref.run(va, fa, vb, fb, q)

@@ -61,6 +61,15 @@ def labelled_tris(tris, labels, remap) -> np.ndarray:
     return rows[o]
 
 
+def float_bits(x) -> np.ndarray:
+    """The bit patterns of float64 values with every NaN written as one NaN. A degenerate construction (an
+    all-coplanar pair's segment) gives NaN on both sides, but x86 and the GPU encode the default NaN
+    differently (sign and payload); every other value must match bit for bit."""
+    y = np.array(x, dtype=np.float64, copy=True)
+    y[np.isnan(y)] = np.nan
+    return y.view(np.int64)
+
+
 def sorted_pairs(p: np.ndarray) -> np.ndarray:
     p = np.asarray(p, dtype=np.int64).reshape(-1, 2)
     return p[np.lexsort((p[:, 1], p[:, 0]))]
@@ -89,8 +98,8 @@ def compare(oracle: dict, gpu: dict, n_orig: int, factor: int, coord_rtol: float
     g1 = np.lexsort((gp[:, 1], gp[:, 0]))
     if op.shape != gp.shape or not np.array_equal(op[o1], gp[g1]):
         bad["intersecting_pairs"] = (len(op), len(gp))
-    elif not np.array_equal(osg[o1].view(np.int64), gsg[g1].view(np.int64)):
-        diff = int(np.count_nonzero(osg[o1] != gsg[g1]))
+    elif not np.array_equal(float_bits(osg[o1]), float_bits(gsg[g1])):
+        diff = int(np.count_nonzero(float_bits(osg[o1]) != float_bits(gsg[g1])))
         bad["segments"] = diff
     if oracle["status"] != 1 or gpu["status"] != 1:
         return bad
@@ -129,7 +138,7 @@ def compare(oracle: dict, gpu: dict, n_orig: int, factor: int, coord_rtol: float
             bad["labels"] = (len(lo), len(lg))
     if strict:
         ov, gv = np.asarray(oracle["newv"]), np.asarray(gpu["newv"])
-        if ov.shape != gv.shape or not np.array_equal(ov.view(np.int64), gv.view(np.int64)):
+        if ov.shape != gv.shape or not np.array_equal(float_bits(ov), float_bits(gv)):
             bad["strict_vertices"] = int(np.count_nonzero(np.any(ov != gv, axis=1))) if ov.shape == gv.shape else -1
         ot, gt = np.asarray(oracle["newt"]).reshape(-1, 3), np.asarray(gpu["newt"]).reshape(-1, 3)
         if ot.shape != gt.shape or not np.array_equal(ot, gt):
@@ -179,10 +188,10 @@ def digests(d: dict, n_orig: int, factor: int) -> dict:
         ip, sg = np.asarray(d["cand"]).reshape(-1, 2)[hit], np.asarray(d["seg"]).reshape(-1, 6)[hit]
     o = np.lexsort((ip[:, 1], ip[:, 0]))
     out["intersecting_pairs"] = _sha(ip[o].astype(np.int64))
-    out["segments"] = _sha(sg[o].astype(np.float64))
+    out["segments"] = _sha(float_bits(sg[o]))
     if out["status"] != 1:
         return out
-    out["vertices"] = _sha(np.asarray(d["newv"], np.float64).reshape(-1, 3))
+    out["vertices"] = _sha(float_bits(np.asarray(d["newv"], np.float64).reshape(-1, 3)))
     out["arrangement"] = _sha(np.asarray(d["newt"], np.int64).reshape(-1, 3))
     labels = np.asarray(d["labels"], np.int64) if gpu else oracle_labels(d)
     out["labels"] = _sha(labels.astype(np.int64))

@@ -50,3 +50,27 @@ def test_port_matches_reference_digests(port, name):
                   "groups_b", "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b"):
             x, y = np.asarray(r[k]), np.asarray(d[k])
             assert x.shape == y.shape and np.array_equal(x, y, equal_nan=x.dtype.kind == "f"), k
+
+
+def test_port_matches_reference_meshes_digests(port):
+    """The reference's own test meshes (tests/golden/reference_meshes.npz): the restatement reproduces the
+    compiled reference's digests at both weld factors."""
+    g = np.load(os.path.join(os.path.dirname(GOLDEN), "reference_meshes.npz"))
+    with open(os.path.join(os.path.dirname(GOLDEN), "reference_meshes_digests.json")) as f:
+        table = json.load(f)
+    for key, want in table.items():
+        name = key.split(":")[0]
+        va, fa, vb, fb = (g[f"{name}:{x}"] for x in ("va", "fa", "vb", "fb"))
+        assert input_digest(va, fa, vb, fb) == want["inputs"]
+        d = port.run(va, fa, vb, fb, want["quantum"])
+        assert digests(d, len(va) + len(vb), want["quantum"]) == {k: v for k, v in want.items()
+                                                                  if k not in ("inputs", "quantum")}, key
+
+
+def test_port_earcut_matches_reference_fixture_file(port):
+    """The reference's earcut fixtures with the reference's indices (tests/golden/earcut_reference_fixtures.npz)."""
+    g = np.load(os.path.join(os.path.dirname(GOLDEN), "earcut_reference_fixtures.npz"))
+    xy, ro, po, idx, io = g["xy"], g["ring_off"], g["poly_off"], g["idx"], g["idx_off"]
+    for p in range(len(po) - 1):
+        rings = [xy[ro[r]:ro[r + 1]] for r in range(po[p], po[p + 1])]
+        assert np.array_equal(port.earcut(rings), idx[io[p]:io[p + 1]]), str(g["names"][p])
