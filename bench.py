@@ -231,6 +231,7 @@ def gpu_arm(args, rank, world, local, dist):
                                            ctypes.byref(hB)), "create B")
         sbg._check(L.sb_boolean_create(hA, hB, ctypes.byref(opts), ctypes.byref(hX)), "boolean")
         stats = sbg.Stats()
+        pair_stage = []  # per timed step: device time of the candidate search and the tri-tri tests
 
         def step():
             # fresh vertex upload marks both meshes unprepared; combine() then rebuilds both meshes'
@@ -262,6 +263,7 @@ def gpu_arm(args, rank, world, local, dist):
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
+            pair_stage.append(stats.stage_ms[0] + stats.stage_ms[1])
         torch.cuda.synchronize()
         barrier(dist)
         launches = L.sb_kernel_launches() - launches0
@@ -277,6 +279,7 @@ def gpu_arm(args, rank, world, local, dist):
                 kern[name] = (tot.value, n.value)
             L.sb_kernel_timing(0)
         st = stats.as_dict()
+        st["pair_stage_ms"] = statistics.mean(pair_stage) if pair_stage else 0.0
         # results for the parity self-check (host copies, outside the timed region)
         res = None
         if precision == "filtered":
@@ -534,6 +537,17 @@ def main():
         "clocks": r["clocks"], "gpu_launches": int(r["launches"]),
         "batch": r["batch"], "adjoint": r["adjoint"],
     }
+    # last, so that a tail of the output shows it: both arithmetic forms side by side, for the whole boolean
+    # and for the tri-pair stage (candidate search + tri-tri tests, device time between the stage events)
+    s32, s64 = st["pair_stage_ms"], r["stats_fp64"]["pair_stage_ms"]
+    line["forms"] = {
+        "filtered": {"ms_per_step": round(r["ms_per_step"], 4), "tri_pairs_per_s": round(r["value"]),
+                     "pair_stage_ms": round(s32, 4), "pair_stage_tri_pairs_per_s": round(C / (s32 / 1e3)),
+                     "sign_fallback_rate": st["sign_fallbacks"] / max(st["sign_tests"], 1)},
+        "fp64": {"ms_per_step": round(r["t64"], 4), "tri_pairs_per_s": round(C / (r["t64"] / 1e3)),
+                 "pair_stage_ms": round(s64, 4), "pair_stage_tri_pairs_per_s": round(C / (s64 / 1e3))},
+        "filtered_over_fp64": {"boolean": round(r["t64"] / r["ms_per_step"], 3),
+                               "pair_stage": round(s64 / s32, 3) if s32 > 0 else None}}
     print(json.dumps(line))
 
 

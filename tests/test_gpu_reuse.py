@@ -1,6 +1,7 @@
 """GPU: one prepared mesh reused by several booleans (the reference's SolidMesh is prepared once and may be
 combined with many others, src/solidmesh.cpp:42-76, src/solidboolean.h:36-37), with preparation and combines
-on different streams; every result must equal a boolean of freshly created meshes."""
+on different streams; every result must equal the oracle's (strict parity) and a boolean of freshly created
+meshes."""
 import ctypes
 
 import numpy as np
@@ -8,6 +9,7 @@ import pytest
 
 import solidboolean_gb300 as sbg
 from solidboolean_gb300 import meshgen as mg
+from parity import compare
 
 pytestmark = pytest.mark.gpu
 
@@ -42,10 +44,23 @@ def _results(L, x):
     if n.value:
         sbg._check(L.sb_result_vertices(x, v.ctypes.data, n.value, ctypes.byref(n)), "sb_result_vertices")
     out["newv"] = v
+
+    def dump(name, dtype, cols):
+        nb = ctypes.c_size_t()
+        sbg._check(L.sb_debug_dump(x, name.encode(), None, 0, ctypes.byref(nb)), "sb_debug_dump")
+        a = np.zeros(nb.value // np.dtype(dtype).itemsize, dtype=dtype)
+        if nb.value:
+            sbg._check(L.sb_debug_dump(x, name.encode(), a.ctypes.data, nb.value, ctypes.byref(nb)), "sb_debug_dump")
+        return a.reshape(-1, cols) if cols > 1 else a
+    out["cand"] = dump("candidates", np.uint32, 2).astype(np.int64)
+    out["isect_pairs"] = dump("intersection_pairs", np.uint32, 2).astype(np.int64)
+    out["isect_segs"] = dump("intersection_segments", np.float64, 6)
+    out["newt"] = dump("arrangement", np.uint32, 3).astype(np.int64)
+    out["labels"] = dump("labels", np.int8, 1)
     return out
 
 
-def test_prepared_mesh_reused_across_booleans_and_streams(gpu_lib):
+def test_prepared_mesh_reused_across_booleans_and_streams(gpu_lib, port):
     L = sbg.lib()
     va, fa, vb, fb = mg.pair_large(1234, 5)
     rng = mg.SplitMix64(99)
@@ -72,10 +87,14 @@ def test_prepared_mesh_reused_across_booleans_and_streams(gpu_lib):
             st = sbg.Stats()
             code = L.sb_combine(x, ctypes.byref(st))
             fresh = sbg.run_boolean(va, fa, v2, f2, WELD)
-            assert (code == sbg.SB_OK) == (fresh["status"] == 1), k
+            ref = port.run(va, fa, v2, f2, WELD)
+            assert (code == sbg.SB_OK) == (fresh["status"] == 1) == (ref["status"] == 1), k
             if code != sbg.SB_OK:
                 continue
             got = _results(L, x)
+            got["status"] = 1
+            bad = compare(ref, got, len(va) + len(v2), WELD, strict=True)
+            assert not bad, (k, bad)
             assert np.array_equal(got["newv"], fresh["newv"]), k
             for name in ("union", "diff", "intersect"):
                 assert np.array_equal(got[name], fresh[name]), (k, name)
