@@ -356,6 +356,14 @@ def gpu_arm(args, rank, world, local, dist):
                  "workers": "tuned by the library (4, 8 or 16 from three 64-pair runs)",
                  "failed_pairs": int(np.count_nonzero(statuses != 0)),
                  "timing": "host wall time of one sb_batch_combine call, host inputs"}
+        # the same pairs in the robustness mode (not the reference's behaviour: scale-relative point-on-edge
+        # bound, finer weld quanta after a failure), reported beside the parity mode
+        t0 = time.perf_counter()
+        rstat, _ = sbg.batch_combine(pairs, workers=0, keep=False, robust=sbg.SB_ROBUST_ALL)
+        t1 = time.perf_counter()
+        batch["robust_mode"] = {"failed_pairs": int(np.count_nonzero(rstat != 0)),
+                                "meshes_per_s": allsum(dist, float(len(pairs))) / allmax(dist, t1 - t0),
+                                "flags": "SB_ROBUST_EDGE_TOLERANCE | SB_ROBUST_WELD_RETRY"}
         if rank == 0 and args.batch_cpu_pairs > 0:
             cores = os.cpu_count() or 1
             sample = pairs[:args.batch_cpu_pairs]

@@ -59,11 +59,28 @@ typedef enum sb_order {
     SB_ORDER_INDEX = 1      /* ascending triangle index (skips building the reference leaf order) */
 } sb_order;
 
+/* Robustness beyond the reference (bit flags of sb_options.robust). With 0, the default, every result is
+ * the reference's. With any flag set, results may differ from the reference's where it would fail. */
+typedef enum sb_robust {
+    /* Point-on-edge test of the re-triangulation with a scale-relative bound, |cross| <= 256 eps L (L + S)
+     * (L: the edge's larger 2D extent, S: the face's largest absolute coordinate), instead of the
+     * reference's absolute |cross| <= eps (src/vector2.h:212-215 with src/double.h:30-33). A cut point
+     * computed on the edge of a large face misses that absolute bound by rounding alone, and the reference
+     * then fails with "Attach point to triangle edge failed" (src/retriangulator.cpp:149-152). */
+    SB_ROBUST_EDGE_TOLERANCE = 1,
+    /* When a combine fails (an SB_FAIL_* status), combine again with the weld factor ten times finer, while
+     * the factor stays <= 1e12 and the largest absolute input coordinate times the factor stays below 2^52
+     * (the quantum must stay coarser than FP64's resolution): cut points that a coarse quantum merges
+     * break the reference's loops (src/solidboolean.cpp:150-158). */
+    SB_ROBUST_WELD_RETRY = 2
+} sb_robust;
+
 typedef struct sb_options {
     int64_t weld_factor; /* PositionKey quantisation factor; the reference uses 100000 (src/positionkey.cpp:25) */
     int32_t precision;   /* sb_precision */
     int32_t order;       /* sb_order */
     void *stream;        /* cudaStream_t */
+    uint32_t robust;     /* sb_robust flags; 0 (default) = the reference's behaviour */
 } sb_options;
 
 typedef struct sb_stats {
@@ -83,6 +100,9 @@ typedef struct sb_stats {
     uint32_t loops;              /* cut loops of the first mesh */
     uint32_t order_fallbacks;    /* cut faces whose place in the reference's processing order could not be
                                     derived (they keep triangle-index order; 0 when the order is exact) */
+    uint32_t attempts;           /* combines run by this call: 1, more after SB_ROBUST_WELD_RETRY retries */
+    uint32_t robust;             /* the sb_robust flags in effect */
+    int64_t weld_factor_used;    /* the weld factor of the last attempt */
     double stage_ms[8];          /* broad, narrow, faces, weld, assemble, groups, sides, fetch (device time) */
 } sb_stats;
 

@@ -24,7 +24,7 @@ REF_ROOT = os.environ.get("SB_REFERENCE_ROOT") or os.path.normpath(os.path.join(
 
 _NAMES_I64 = ["status", "cand", "isect", "newt", "groups_a_off", "groups_a", "groups_b_off", "groups_b",
               "sides_a", "sides_b", "union", "diff", "intersect", "leaforder_a", "leaforder_b", "ctx_a", "ctx_b",
-              "loops_a_off", "loops_a", "tri_ranges"]
+              "loops_a_off", "loops_a", "tri_ranges", "attempts", "weld_factor_used"]
 _NAMES_F64 = ["seg", "newv", "time_ms"]
 _SHAPES = {"cand": (-1, 2), "seg": (-1, 6), "newv": (-1, 3), "newt": (-1, 3), "union": (-1, 3),
            "diff": (-1, 3), "intersect": (-1, 3)}
@@ -53,13 +53,22 @@ class Checker:
         L.sbo_tritri.restype = ctypes.c_int
         L.sbo_tritri.argtypes = [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
 
-    def run(self, va, fa, vb, fb, quantum: int = 100000) -> dict:
+    def run(self, va, fa, vb, fb, quantum: int = 100000, robust: int = 0) -> dict:
+        """One boolean. robust: the robust mode's flags (sb_robust; the restatement only, which checks that
+        mode: the reference has none), 0 for the reference's behaviour."""
         va = np.ascontiguousarray(va, dtype=np.float64)
         vb = np.ascontiguousarray(vb, dtype=np.float64)
         fa = np.ascontiguousarray(fa, dtype=np.uint32)
         fb = np.ascontiguousarray(fb, dtype=np.uint32)
-        h = self.lib.sbo_run(va.ctypes.data, len(va), fa.ctypes.data, len(fa),
-                             vb.ctypes.data, len(vb), fb.ctypes.data, len(fb), int(quantum))
+        args = (va.ctypes.data, len(va), fa.ctypes.data, len(fa), vb.ctypes.data, len(vb), fb.ctypes.data,
+                len(fb), int(quantum))
+        if robust:
+            f = self.lib.sbo_run_robust
+            f.restype = ctypes.c_void_p
+            f.argtypes = self.lib.sbo_run.argtypes + [ctypes.c_int]
+            h = f(*args, int(robust))
+        else:
+            h = self.lib.sbo_run(*args)
         out = {}
         try:
             for names, dt, getter in ((_NAMES_I64, np.int64, self.lib.sbo_get_i64),

@@ -49,6 +49,9 @@ namespace port {
 
 static const double kEps = std::numeric_limits<double>::epsilon();
 static long g_factor = 100000;
+// sb_robust flags of the run (include/solidboolean_gb300.h): bit 0 = scale-relative point-on-edge test.
+// Not part of the reference: the robust mode's own checker. 0 = the reference's behaviour.
+static int g_robust = 0;
 
 struct V3 {
     double x = 0, y = 0, z = 0;
@@ -493,9 +496,15 @@ static int intersect(const double *p1, const double *q1, const double *r1, const
 // ---------------------------------------------------------------------------------------------------
 typedef std::unordered_map<size_t, std::unordered_set<size_t>> NeighborMap;
 
-static inline bool onLine(const V2 &p, const V2 &a, const V2 &b)
+static inline bool onLine(const V2 &p, const V2 &a, const V2 &b, double faceScale)
 {
-    return std::abs(std::abs((p.y - a.y) * (b.x - a.x) - (p.x - a.x) * (b.y - a.y))) <= kEps;
+    const double cr = std::abs(std::abs((p.y - a.y) * (b.x - a.x) - (p.x - a.x) * (b.y - a.y)));
+    if (!(g_robust & 1))
+        return cr <= kEps; // src/vector2.h:212-215, src/double.h:30-33
+    // robust mode (not the reference): 256 eps L (L + S), L the edge's larger 2D extent, S the face's largest
+    // absolute corner coordinate
+    const double L = std::max(std::abs(b.x - a.x), std::abs(b.y - a.y));
+    return cr <= (256.0 * kEps) * (L * (L + faceScale));
 }
 static inline bool inPolygon(const V2 &p, const std::vector<V2> &pts, const std::vector<size_t> &poly)
 {
@@ -512,6 +521,7 @@ static inline bool inPolygon(const V2 &p, const std::vector<V2> &pts, const std:
 
 struct ReTri {
     V3 axis, origin, normal;
+    double faceScale = 0.0; // largest absolute corner coordinate (robust mode only)
     std::vector<V2> pts;
     const NeighborMap *nbr = nullptr;
     std::vector<std::vector<size_t>> polylines, inner, polygons, tris;
@@ -531,6 +541,8 @@ struct ReTri {
     {
         axis = normalized(corners[1] - corners[0]);
         origin = corners[0];
+        for (const auto &c : corners)
+            faceScale = std::max(faceScale, std::max(std::abs(c.x), std::max(std::abs(c.y), std::abs(c.z))));
         project(corners);
     }
     void setEdges(const std::vector<V3> &p, const NeighborMap *m)
@@ -584,7 +596,7 @@ struct ReTri {
     int attach(const V2 &p)
     {
         for (int i = 0; i < 3; ++i)
-            if (onLine(p, pts[i], pts[(i + 1) % 3]))
+            if (onLine(p, pts[i], pts[(i + 1) % 3], faceScale))
                 return i;
         return -1;
     }
@@ -1119,8 +1131,8 @@ struct Boolean {
 
 using namespace port;
 
-extern "C" void *sbo_run(const double *va, size_t nva, const uint32_t *ta, size_t nta, const double *vb, size_t nvb,
-                         const uint32_t *tb, size_t ntb, long quantum)
+static sbo::Dump *run_once(const double *va, size_t nva, const uint32_t *ta, size_t nta, const double *vb,
+                           size_t nvb, const uint32_t *tb, size_t ntb, long quantum)
 {
     using C = std::chrono::steady_clock;
     g_factor = quantum;
@@ -1217,6 +1229,45 @@ extern "C" void *sbo_run(const double *va, size_t nva, const uint32_t *ta, size_
     auto ms = [](C::time_point x, C::time_point y) { return std::chrono::duration<double, std::milli>(y - x).count(); };
     d->f64["time_ms"] = {ms(t0, t1), ms(t1, t2), sb.tm[0], sb.tm[1], sb.tm[2], sb.tm[3], sb.tm[4], sb.tm[5], sb.tm[6]};
     g_factor = 100000;
+    return d;
+}
+
+extern "C" void *sbo_run(const double *va, size_t nva, const uint32_t *ta, size_t nta, const double *vb, size_t nvb,
+                         const uint32_t *tb, size_t ntb, long quantum)
+{
+    g_robust = 0;
+    return run_once(va, nva, ta, nta, vb, nvb, tb, ntb, quantum);
+}
+
+// The robust mode's checker (not the reference): flags bit 0 = scale-relative point-on-edge test, bit 1 =
+// after a failed combine, combine again with the quantum ten times finer while it stays <= 1e12 and the
+// largest absolute coordinate of a triangle corner times it stays below 2^52.
+extern "C" void *sbo_run_robust(const double *va, size_t nva, const uint32_t *ta, size_t nta, const double *vb,
+                                size_t nvb, const uint32_t *tb, size_t ntb, long quantum, int flags)
+{
+    g_robust = flags;
+    sbo::Dump *d = run_once(va, nva, ta, nta, vb, nvb, tb, ntb, quantum);
+    long attempts = 1;
+    if ((flags & 2) && d->i64["status"][0] == 0) {
+        double maxAbs = 0.0;
+        auto scan = [&](const double *v, const uint32_t *t, size_t nt) {
+            for (size_t i = 0; i < 3 * nt; ++i)
+                for (int k = 0; k < 3; ++k)
+                    maxAbs = std::max(maxAbs, std::abs(v[3 * (size_t)t[i] + k]));
+        };
+        scan(va, ta, nta);
+        scan(vb, tb, ntb);
+        while (d->i64["status"][0] == 0 && quantum <= 100000000000L &&
+               maxAbs * (double)(quantum * 10) < 4503599627370496.0) {
+            quantum *= 10;
+            delete d;
+            d = run_once(va, nva, ta, nta, vb, nvb, tb, ntb, quantum);
+            ++attempts;
+        }
+    }
+    d->i64["attempts"] = {attempts};
+    d->i64["weld_factor_used"] = {quantum};
+    g_robust = 0;
     return d;
 }
 

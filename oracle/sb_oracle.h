@@ -31,6 +31,9 @@ extern "C" {
 
 void *sbo_run(const double *va, size_t nva, const uint32_t *ta, size_t nta,
               const double *vb, size_t nvb, const uint32_t *tb, size_t ntb, long quantum);
+/* The same with the robust mode's flags (sb_robust in include/solidboolean_gb300.h; not the reference). */
+void *sbo_run_robust(const double *va, size_t nva, const uint32_t *ta, size_t nta,
+                     const double *vb, size_t nvb, const uint32_t *tb, size_t ntb, long quantum, int flags);
 long sbo_len(void *h, const char *name);
 int sbo_get_i64(void *h, const char *name, int64_t *out);
 int sbo_get_f64(void *h, const char *name, double *out);

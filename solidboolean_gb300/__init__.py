@@ -27,6 +27,9 @@ SB_ERR_INVALID, SB_ERR_CUDA, SB_ERR_CAPACITY, SB_ERR_NOT_COMBINED = 10, 11, 12, 
 SB_UNION, SB_DIFF, SB_INTERSECT = 0, 1, 2
 PRECISION = {"filtered": 0, "fp64": 1}
 ORDER = {"reference": 0, "index": 1}
+# sb_robust flags (include/solidboolean_gb300.h): 0 keeps the reference's behaviour
+SB_ROBUST_EDGE_TOLERANCE, SB_ROBUST_WELD_RETRY = 1, 2
+SB_ROBUST_ALL = SB_ROBUST_EDGE_TOLERANCE | SB_ROBUST_WELD_RETRY
 
 EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_kernel_launches", "sb_mesh_create",
            "sb_mesh_create_device",
@@ -37,7 +40,7 @@ EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_kernel
 
 class Options(ctypes.Structure):
     _fields_ = [("weld_factor", ctypes.c_int64), ("precision", ctypes.c_int32), ("order", ctypes.c_int32),
-                ("stream", ctypes.c_void_p)]
+                ("stream", ctypes.c_void_p), ("robust", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -50,7 +53,8 @@ class Stats(ctypes.Structure):
                 ("regions_second", ctypes.c_uint32), ("failed_faces", ctypes.c_uint32),
                 ("loop_vertices", ctypes.c_uint32), ("loop_bad_degree", ctypes.c_uint32),
                 ("duplicate_halfedges", ctypes.c_uint32), ("loops", ctypes.c_uint32),
-                ("order_fallbacks", ctypes.c_uint32), ("stage_ms", ctypes.c_double * 8)]
+                ("order_fallbacks", ctypes.c_uint32), ("attempts", ctypes.c_uint32), ("robust", ctypes.c_uint32),
+                ("weld_factor_used", ctypes.c_int64), ("stage_ms", ctypes.c_double * 8)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}
@@ -129,13 +133,14 @@ def _check(code: int, what: str) -> int:
 
 
 def make_options(weld_factor: int = 100000, precision: str = "filtered", order: str = "reference",
-                 stream: int | None = None) -> Options:
+                 stream: int | None = None, robust: int = 0) -> Options:
     o = Options()
     lib().sb_default_options(ctypes.byref(o))
     o.weld_factor = int(weld_factor)
     o.precision = PRECISION[precision]
     o.order = ORDER[order]
     o.stream = stream or None
+    o.robust = int(robust)
     return o
 
 
@@ -271,9 +276,9 @@ class SolidBoolean:
 
 
 def run_boolean(va, fa, vb, fb, weld_factor: int = 100000, precision: str = "filtered",
-                order: str = "reference") -> dict:
+                order: str = "reference", robust: int = 0) -> dict:
     """One boolean with every result and stage dump copied to the host (used by tests and smoke)."""
-    opts = make_options(weld_factor, precision, order)
+    opts = make_options(weld_factor, precision, order, robust=robust)
     a = SolidMesh(opts)
     a.setVertices(va)
     a.setTriangles(fa)
@@ -301,7 +306,7 @@ OP_CODES = {"union": SB_UNION, "diff": SB_DIFF, "intersect": SB_INTERSECT}
 
 
 def batch_combine(pairs, weld_factor: int = 100000, precision: str = "filtered", order: str = "reference",
-                  workers: int = 0, keep: bool = True):
+                  workers: int = 0, keep: bool = True, robust: int = 0):
     """Many independent booleans in one call (sb_batch_combine). pairs: sequence of (va, fa, vb, fb, op) with
     op in "union" / "diff" / "intersect". Returns (statuses, results): statuses an int32 array of per-pair
     sb_combine codes; results (when keep) a list of (result vertices, the op's triangles) per pair, empty
@@ -323,7 +328,7 @@ def batch_combine(pairs, weld_factor: int = 100000, precision: str = "filtered",
     tb, tbo = csr([p[3] for p in pairs], 3, np.uint32)
     ops = np.array([OP_CODES[p[4]] for p in pairs], dtype=np.int32)
     statuses = np.zeros(n, dtype=np.int32)
-    opts = make_options(weld_factor, precision, order)
+    opts = make_options(weld_factor, precision, order, robust=robust)
     handle = ctypes.c_void_p()
     ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     code = L.sb_batch_combine(n, ptr(va), ptr(vao), ptr(ta), ptr(tao), ptr(vb), ptr(vbo), ptr(tb), ptr(tbo),

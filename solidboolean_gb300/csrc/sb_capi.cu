@@ -1070,6 +1070,7 @@ sb_status combine_impl(sb_boolean *b)
         fa.faceNtris = faceNtris;
         fa.faceNedges = faceNedges;
         fa.ptSrc = ptSrc;
+        fa.robustEdges = (b->opts.robust & SB_ROBUST_EDGE_TOLERANCE) != 0;
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }
@@ -1524,6 +1525,7 @@ void sb_default_options(sb_options *o)
     o->precision = SB_PRECISION_FILTERED;
     o->order = SB_ORDER_REFERENCE;
     o->stream = nullptr;
+    o->robust = 0;
 }
 
 const char *sb_status_string(sb_status s)
@@ -1765,6 +1767,28 @@ sb_status sb_boolean_create(const sb_mesh *first, const sb_mesh *second, const s
     });
 }
 
+static bool is_combine_failure(sb_status r)
+{
+    return r == SB_FAIL_ATTACH || r == SB_FAIL_LINK || r == SB_FAIL_LOOP;
+}
+
+// Largest absolute vertex coordinate of a prepared mesh: its hierarchy's root box (FP64 unions of the
+// triangle boxes, which hold the vertices' exact minima and maxima). Synchronises the stream.
+static sb_status mesh_max_abs(const sb_mesh *m, cudaStream_t s, double *out)
+{
+    const MeshDev &d = m->d;
+    *out = 0.0;
+    if (d.nt <= 0)
+        return SB_OK;
+    double box[6];
+    const double *src = d.nt == 1 ? d.box64 : d.nbox64; // node 0 is the root
+    SB_CUDA_CHECK(cudaMemcpyAsync(box, src, sizeof box, cudaMemcpyDeviceToHost, s));
+    SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    for (double x : box)
+        *out = std::max(*out, std::fabs(x));
+    return SB_OK;
+}
+
 sb_status sb_combine(sb_boolean *b, sb_stats *stats)
 {
     if (!b)
@@ -1793,6 +1817,28 @@ sb_status sb_combine(sb_boolean *b, sb_stats *stats)
                     return r;
             }
         sb_status r = combine_impl(b);
+        uint32_t attempts = 1;
+        const int64_t factor0 = b->opts.weld_factor;
+        if (is_combine_failure(r) && (b->opts.robust & SB_ROBUST_WELD_RETRY)) {
+            // the finer quanta: x10 while the factor stays <= 1e12 and coarser than FP64's resolution
+            double absA = 0.0, absB = 0.0;
+            sb_status e = mesh_max_abs(ma, b->s, &absA);
+            if (e == SB_OK)
+                e = mesh_max_abs(mb, b->s, &absB);
+            if (e != SB_OK)
+                return e;
+            const double maxAbs = std::max(absA, absB);
+            while (is_combine_failure(r) && b->opts.weld_factor <= 100000000000LL &&
+                   maxAbs * (double)(b->opts.weld_factor * 10) < 4503599627370496.0) {
+                b->opts.weld_factor *= 10;
+                r = combine_impl(b);
+                ++attempts;
+            }
+        }
+        b->stats.attempts = attempts;
+        b->stats.robust = b->opts.robust;
+        b->stats.weld_factor_used = b->opts.weld_factor;
+        b->opts.weld_factor = factor0; // the next combine starts from the caller's factor again
         if (stats)
             *stats = b->stats;
         return r;

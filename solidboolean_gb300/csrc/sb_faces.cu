@@ -145,9 +145,19 @@ SB_HDF void ordered_keys(const int *src, int n, FacePtrs &s, int *dst)
         dst[i] = src[s.horder[i]];
 }
 
-SB_HD bool on_line(d2 p, d2 a, d2 b)
+// Point-on-edge test of the polyline ends. The reference's bound is absolute: |cross| <= eps
+// (src/vector2.h:212-215, src/double.h:30-33). With robust set, the bound scales with the edge and the face's
+// coordinates: 256 eps L (L + S), L the edge's larger 2D extent, S the face's largest absolute 3D coordinate
+// (a cut point on the edge carries rounding of order eps S from its construction and projection, and the
+// cross product multiplies it by the edge's length). 256 eps is a power of two, so the bound is formed by
+// the same roundings on every machine.
+SB_HD bool on_line(d2 p, d2 a, d2 b, bool robust, double S)
 {
-    return fabs(fabs((p.y - a.y) * (b.x - a.x) - (p.x - a.x) * (b.y - a.y))) <= kDblEps;
+    const double cr = fabs(fabs((p.y - a.y) * (b.x - a.x) - (p.x - a.x) * (b.y - a.y)));
+    if (!robust)
+        return cr <= kDblEps;
+    const double L = fmax(fabs(b.x - a.x), fabs(b.y - a.y));
+    return cr <= (256.0 * kDblEps) * (L * (L + S));
 }
 
 // pnpoly over a ring of local ids (src/vector2.h:199-210)
@@ -271,6 +281,9 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
         const double *p = M.v + 3 * (size_t)M.t[3 * (size_t)job.tri + k];
         c[k] = mk(p[0], p[1], p[2]);
     }
+    double faceScale = 0.0; // largest absolute corner coordinate (the robust point-on-edge bound)
+    for (int k = 0; k < 3; ++k)
+        faceScale = fmax(faceScale, fmax(fabs(c[k].x), fmax(fabs(c[k].y), fabs(c[k].z))));
     d3 normal = unit_normal(c[0], c[1], c[2]);
     d3 axis = normalized(c[1] - c[0]);
     d3 perp = cross(normal, axis);
@@ -345,10 +358,10 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
         int front = s.linePts[L0], back = s.linePts[L1 - 1];
         int fe = -1, be = -1;
         for (int e = 0; e < 3 && fe < 0; ++e)
-            if (on_line(s.pts2[front], s.pts2[e], s.pts2[(e + 1) % 3]))
+            if (on_line(s.pts2[front], s.pts2[e], s.pts2[(e + 1) % 3], a.robustEdges != 0, faceScale))
                 fe = e;
         for (int e = 0; e < 3 && be < 0; ++e)
-            if (on_line(s.pts2[back], s.pts2[e], s.pts2[(e + 1) % 3]))
+            if (on_line(s.pts2[back], s.pts2[e], s.pts2[(e + 1) % 3], a.robustEdges != 0, faceScale))
                 be = e;
         if (fe < 0 || be < 0) {
             res.status = 1;

@@ -26,6 +26,7 @@ struct FaceArgs {
                                                // neighbour-map iteration order, both directions
     int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
     int *ptSrc = nullptr; // optional, per face point: 2 x (intersecting pair) + segment end it came from
+    int robustEdges = 0;  // SB_ROBUST_EDGE_TOLERANCE: scale-relative point-on-edge test (0: the reference's)
 };
 
 size_t face_scratch_bytes_host(int np);
