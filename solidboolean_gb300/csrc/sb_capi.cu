@@ -288,6 +288,58 @@ __global__ void k_pair_keys(int K, const unsigned int *dK, const int *__restrict
     pairPerm[j] = perm[idx];
 }
 
+// Each cut face's pairs in the reference's processing order. Its dual traversal reaches a first-mesh face's
+// pairs in the second tree's leaf order and a second-mesh face's in the first tree's, so a face's pairs sort by
+// the other triangle's leaf position. The faces are grouped before the leaf orders are ready (pairs listed by
+// the other triangle's index); then one thread per face sorts its list in place, in registers for up to
+// kPairSortLocal pairs (the usual case: two or three), else in global memory.
+constexpr int kPairSortLocal = 48;
+__global__ void k_face_pair_order(int nFaces, int FA, const int *__restrict__ faceBegin, int *pairIdx,
+                                  const uint32_t *__restrict__ pairAB, const int *__restrict__ rankA,
+                                  const int *__restrict__ rankB)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nFaces)
+        return;
+    const int side = f >= FA ? 1 : 0;
+    const int *rank = side ? rankA : rankB; // the other mesh's leaf positions
+    const int b0 = faceBegin[f], n = faceBegin[f + 1] - b0;
+    auto keyOf = [&](int pair) -> uint64_t {
+        const uint32_t other = pairAB[2 * (size_t)pair + (side ? 0 : 1)];
+        return ((uint64_t)(uint32_t)rank[other] << 32) | (uint32_t)pair;
+    };
+    if (n <= 1)
+        return;
+    if (n <= kPairSortLocal) {
+        uint64_t v[kPairSortLocal];
+        for (int i = 0; i < n; ++i) {
+            const uint64_t x = keyOf(pairIdx[b0 + i]);
+            int j = i - 1;
+            while (j >= 0 && v[j] > x) {
+                v[j + 1] = v[j];
+                --j;
+            }
+            v[j + 1] = x;
+        }
+        for (int i = 0; i < n; ++i)
+            pairIdx[b0 + i] = (int)(uint32_t)v[i];
+        return;
+    }
+    for (int i = 1; i < n; ++i) {
+        const int pi = pairIdx[b0 + i];
+        const uint64_t ki = keyOf(pi);
+        int j = i - 1;
+        while (j >= 0) {
+            const int pj = pairIdx[b0 + j];
+            if (keyOf(pj) <= ki)
+                break;
+            pairIdx[b0 + j + 1] = pj;
+            --j;
+        }
+        pairIdx[b0 + j + 1] = pi;
+    }
+}
+
 __global__ void k_hi32(int n, const uint64_t *__restrict__ k, int *out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -845,11 +897,16 @@ sb_status combine_impl(sb_boolean *b)
     uint32_t *pairPerm = (uint32_t *)(ib + o_pp);
     b->d_pairPerm = pairPerm;
     b->d_segK = segK;
-    // the leaf orders may still be building on the meshes' second streams (they overlap the broad and
-    // narrow phases); from here on the stream waits for them
-    for (const sb_mesh *cm : {b->first, b->second})
-        if (cm->rankPending && cm->aux)
-            SB_CUDA_CHECK(cudaStreamWaitEvent(s, cm->auxJoin, 0));
+    // The leaf orders may still be building on the meshes' second streams (they overlap the broad and narrow
+    // phases). Nothing before the re-triangulation needs them: the pairs are grouped by face, the faces
+    // counted and their capacities sized, and the arrangement's uncut parts prepared first; the stream waits
+    // for the leaf orders only before the pairs of each face are put in the reference's order.
+    auto waitRanks = [&]() -> sb_status {
+        for (const sb_mesh *cm : {b->first, b->second})
+            if (cm->rankPending && cm->aux)
+                SB_CUDA_CHECK(cudaStreamWaitEvent(s, cm->auxJoin, 0));
+        return SB_OK;
+    };
     auto rankResults = [&]() -> sb_status {
         for (const sb_mesh *cm : {b->first, b->second}) {
             const sb_status r = reference_rank_result(const_cast<sb_mesh *>(cm));
@@ -861,9 +918,8 @@ sb_status combine_impl(sb_boolean *b)
     const bool useRank = b->opts.order == SB_ORDER_REFERENCE && A.rankValid && B.rankValid;
     int FA = 0, FB = 0;
     if (Kcap > 0) {
-        SB_COUNT(k_pair_keys)<<<blocks(Kcap, 256), 256, 0, s>>>((int)Kcap, dK, sel, candSorted, nB,
-                                                      useRank ? A.rank : nullptr, useRank ? B.rank : nullptr, seg,
-                                                      perm, keyA, keyB, val, segK, pairAB, pairPerm);
+        SB_COUNT(k_pair_keys)<<<blocks(Kcap, 256), 256, 0, s>>>((int)Kcap, dK, sel, candSorted, nB, nullptr, nullptr,
+                                                      seg, perm, keyA, keyB, val, segK, pairAB, pairPerm);
         if (Kcap <= (unsigned int)kGroupMax) {
             const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
             const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
@@ -900,12 +956,6 @@ sb_status combine_impl(sb_boolean *b)
     }
     b->K = (int)K;
     st.intersecting_pairs = K;
-    {
-        // synchronised past the leaf orders (when there were pairs to group; else at the end)
-        const sb_status r = K > 0 ? rankResults() : SB_OK;
-        if (r != SB_OK)
-            return r;
-    }
     const int nFaces = FA + FB;
     st.cut_faces_first = FA;
     st.cut_faces_second = FB;
@@ -933,6 +983,10 @@ sb_status combine_impl(sb_boolean *b)
     int *faceRank = nullptr, *faceByRank = nullptr, *ptRef = nullptr, *edgeRef = nullptr, *retriRef = nullptr;
     int *rankTmp[3] = {nullptr, nullptr, nullptr}, *rankTot = nullptr;
     bool orderPending = false;
+    FaceOrderArgs fo;   // the faces' processing order (second stream), set up with the face capacities
+    RankScanArgs ra;
+    char *ob = nullptr;
+    size_t o_fks = 0, o_fvs = 0;
     if (nFaces > 0) {
         SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
         SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
@@ -954,8 +1008,10 @@ sb_status combine_impl(sb_boolean *b)
         // the reference's processing order of the cut faces: each face keyed by its first pair's place in the
         // tree traversal, sorted, then ordered like the context map iterates them
         Carve co;
-        const size_t o_fk = co.take<unsigned long long>(nFaces), o_fks = co.take<unsigned long long>(nFaces);
-        const size_t o_fv = co.take<int>(nFaces), o_fvs = co.take<int>(nFaces);
+        const size_t o_fk = co.take<unsigned long long>(nFaces);
+        o_fks = co.take<unsigned long long>(nFaces);
+        const size_t o_fv = co.take<int>(nFaces);
+        o_fvs = co.take<int>(nFaces);
         const size_t o_fr = co.take<int>(nFaces + 1), o_fbr = co.take<int>(nFaces + 1);
         const size_t o_ik = co.take<uint32_t>(nFaces + 1);
         const size_t o_hA = co.take<int>(hash_scratch_ints(FA)), o_hB = co.take<int>(hash_scratch_ints(FB));
@@ -963,8 +1019,7 @@ sb_status combine_impl(sb_boolean *b)
         const size_t o_t0 = co.take<int>(nFaces + 1), o_t1 = co.take<int>(nFaces + 1), o_t2 = co.take<int>(nFaces + 1);
         const size_t o_tot = co.take<int>(8);
         SB_CUDA_CHECK(b->order.ensure(co.off));
-        char *ob = b->order.as<char>();
-        FaceOrderArgs fo;
+        ob = b->order.as<char>();
         fo.nFaces = nFaces;
         fo.FA = FA;
         fo.FB = FB;
@@ -993,7 +1048,6 @@ sb_status combine_impl(sb_boolean *b)
         rankTmp[1] = (int *)(ob + o_t1);
         rankTmp[2] = (int *)(ob + o_t2);
         rankTot = (int *)(ob + o_tot);
-        RankScanArgs ra;
         std::memset(&ra, 0, sizeof ra);
         ra.n = nFaces;
         ra.FA = FA;
@@ -1020,6 +1074,68 @@ sb_status combine_impl(sb_boolean *b)
         totals[1] = pTot;
         totals[2] = tTot;
         totals[3] = eTot;
+    }
+    AsmArgs g;
+    std::memset(&g, 0, sizeof g);
+    g.nFaces = nFaces;
+    g.faceSide = faceSide;
+    g.faceTri = faceTri;
+    // ---------------- arrangement ----------------
+    Carve ca;
+    size_t o_cA = ca.take<int>(nA + 1), o_cB = ca.take<int>(nB + 1), o_nA = ca.take<int>(nA + 1);
+    size_t o_nB = ca.take<int>(nB + 1), o_rA = ca.take<int>(nA + 1), o_rB = ca.take<int>(nB + 1);
+    SB_CUDA_CHECK(b->arr.ensure(ca.off));
+    char *ab = b->arr.as<char>();
+    g.cutA = (int *)(ab + o_cA);
+    g.cutB = (int *)(ab + o_cB);
+    int *notA = (int *)(ab + o_nA), *notB = (int *)(ab + o_nB);
+    g.uncutRankA = (int *)(ab + o_rA);
+    g.uncutRankB = (int *)(ab + o_rB);
+    {
+        Fills fl(s);
+        fl.i32(g.cutA, nA + 1, 0);
+        fl.i32(g.cutB, nB + 1, 0);
+        fl.i32(notA, nA + 1, 0);
+        fl.i32(notB, nB + 1, 0);
+        fl.launch();
+    }
+    launch_mark_cut(g, s);
+    g.truncOcc = d_truncOcc;
+    for (int side = 0; side < 2; ++side) {
+        // a mesh holding a directed edge twice: find where the reference's uncut-triangle insertion stops
+        const MeshDev &M = side == 0 ? A : B;
+        if (adjDup[side] == 0 || M.nt == 0)
+            continue;
+        const uint32_t cap = pow2_at_least(2 * 3 * (size_t)M.nt);
+        SB_CUDA_CHECK(b->trunc.ensure((sizeof(uint64_t) + sizeof(int)) * (size_t)cap));
+        uint64_t *tk = b->trunc.as<uint64_t>();
+        int *tv = reinterpret_cast<int *>(tk + cap);
+        SB_CUDA_CHECK(cudaMemsetAsync(tk, 0xFF, sizeof(uint64_t) * cap, s));
+        SB_CUDA_CHECK(cudaMemsetAsync(tv, 0x7F, sizeof(int) * cap, s));
+        const int *cutM = side == 0 ? g.cutA : g.cutB;
+        SB_COUNT(k_trunc_insert)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1);
+        SB_COUNT(k_trunc_find)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1, d_truncOcc + side);
+    }
+    if (nA > 0)
+        SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA, d_truncOcc);
+    if (nB > 0)
+        SB_COUNT(k_not_flag)<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB, d_truncOcc + 1);
+    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notA, g.uncutRankA, nA + 1, s);
+    }));
+    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notB, g.uncutRankB, nB + 1, s);
+    }));
+    // from here on the leaf orders are needed
+    {
+        const sb_status r = waitRanks();
+        if (r != SB_OK)
+            return r;
+    }
+    if (nFaces > 0) {
+        if (useRank)
+            SB_COUNT(k_face_pair_order)<<<blocks(nFaces, 128), 128, 0, s>>>(nFaces, FA, faceBegin, pairIdx, pairAB,
+                                                                          A.rank, B.rank);
         // the processing order runs on the second stream beside the re-triangulation (the weld waits for it)
         cudaStream_t so = b->side;
         SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
@@ -1084,8 +1200,6 @@ sb_status combine_impl(sb_boolean *b)
         SB_COUNT(k_face_status)<<<blocks(nFaces, 256), 256, 0, s>>>(nFaces, faceSide, faceStatus, d_firstFail);
 
     // ---------------- global weld ----------------
-    AsmArgs g;
-    std::memset(&g, 0, sizeof g);
     g.A = A;
     g.B = B;
     g.factor = factor;
@@ -1141,52 +1255,6 @@ sb_status combine_impl(sb_boolean *b)
     // the number of welded points is read with the arrangement's counts below (nothing before needs it)
     int nNew = 0;
 
-    // ---------------- arrangement ----------------
-    Carve ca;
-    size_t o_cA = ca.take<int>(nA + 1), o_cB = ca.take<int>(nB + 1), o_nA = ca.take<int>(nA + 1);
-    size_t o_nB = ca.take<int>(nB + 1), o_rA = ca.take<int>(nA + 1), o_rB = ca.take<int>(nB + 1);
-    SB_CUDA_CHECK(b->arr.ensure(ca.off));
-    char *ab = b->arr.as<char>();
-    g.cutA = (int *)(ab + o_cA);
-    g.cutB = (int *)(ab + o_cB);
-    int *notA = (int *)(ab + o_nA), *notB = (int *)(ab + o_nB);
-    g.uncutRankA = (int *)(ab + o_rA);
-    g.uncutRankB = (int *)(ab + o_rB);
-    {
-        Fills fl(s);
-        fl.i32(g.cutA, nA + 1, 0);
-        fl.i32(g.cutB, nB + 1, 0);
-        fl.i32(notA, nA + 1, 0);
-        fl.i32(notB, nB + 1, 0);
-        fl.launch();
-    }
-    launch_mark_cut(g, s);
-    g.truncOcc = d_truncOcc;
-    for (int side = 0; side < 2; ++side) {
-        // a mesh holding a directed edge twice: find where the reference's uncut-triangle insertion stops
-        const MeshDev &M = side == 0 ? A : B;
-        if (adjDup[side] == 0 || M.nt == 0)
-            continue;
-        const uint32_t cap = pow2_at_least(2 * 3 * (size_t)M.nt);
-        SB_CUDA_CHECK(b->trunc.ensure((sizeof(uint64_t) + sizeof(int)) * (size_t)cap));
-        uint64_t *tk = b->trunc.as<uint64_t>();
-        int *tv = reinterpret_cast<int *>(tk + cap);
-        SB_CUDA_CHECK(cudaMemsetAsync(tk, 0xFF, sizeof(uint64_t) * cap, s));
-        SB_CUDA_CHECK(cudaMemsetAsync(tv, 0x7F, sizeof(int) * cap, s));
-        const int *cutM = side == 0 ? g.cutA : g.cutB;
-        SB_COUNT(k_trunc_insert)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1);
-        SB_COUNT(k_trunc_find)<<<blocks(M.nt, 256), 256, 0, s>>>(M.nt, M.t, cutM, tk, tv, cap - 1, d_truncOcc + side);
-    }
-    if (nA > 0)
-        SB_COUNT(k_not_flag)<<<blocks(nA, 256), 256, 0, s>>>(nA, g.cutA, notA, d_truncOcc);
-    if (nB > 0)
-        SB_COUNT(k_not_flag)<<<blocks(nB, 256), 256, 0, s>>>(nB, g.cutB, notB, d_truncOcc + 1);
-    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notA, g.uncutRankA, nA + 1, s);
-    }));
-    SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-        return cub::DeviceScan::ExclusiveSum(tmp, bytes, notB, g.uncutRankB, nB + 1, s);
-    }));
     if (nFaces > 0) {
         // the re-triangulated triangles are numbered in the faces' processing order
         RankScanArgs ra;
@@ -1213,6 +1281,12 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(rb.add(firstFail, d_firstFail, sizeof firstFail));
         SB_CUDA_CHECK(rb.add(&nNew, g.firstRank + nSeq, sizeof nNew));
         SB_CUDA_CHECK(rb.sync());
+    }
+    {
+        // synchronised past the stream's wait for the leaf orders: their status is readable
+        const sb_status r = rankResults();
+        if (r != SB_OK)
+            return r;
     }
     g.nNew = nNew;
     st.new_points = (uint64_t)nNew;
