@@ -1414,6 +1414,7 @@ sb_status combine_impl(sb_boolean *b)
     const size_t o_rsn = cl.take<int>(nTriS), o_rsx = cl.take<int>(nTriS), o_bg = cl.take<int>(nTriS);
     const size_t o_be = cl.take<int>(nTriS), o_f0 = cl.take<int>(nTriS), o_f1 = cl.take<int>(nTriS);
     const size_t o_tg = cl.take<int>(3 * nTriS), o_ffl = cl.take<int>(std::max(3 * nTriS, 4 * nNewS) + 1);
+    const size_t o_any = cl.take<int>(1);
     SB_CUDA_CHECK(b->flood.ensure(cl.off));
     char *lb = b->flood.as<char>();
     LoopOrderArgs lo;
@@ -1470,6 +1471,7 @@ sb_status combine_impl(sb_boolean *b)
     fd.front1 = (int *)(lb + o_f1);
     fd.tgt = (int *)(lb + o_tg);
     fd.flag = (int *)(lb + o_ffl);
+    fd.anyMixed = (int *)(lb + o_any);
     fd.errors = d_counters + kCntSideErrors;
     {
         Fills fl(s);
@@ -1479,6 +1481,7 @@ sb_status combine_impl(sb_boolean *b)
         fl.i32(fd.rsMax, nTriS, -1);
         fl.i32(fd.bfsGroup, nTriS, -1);
         fl.i32(fd.best, nTriS, INT_MAX);
+        fl.i32(fd.anyMixed, 1, 0);
         fl.launch();
     }
     // the loop order needs the loop and half-edge tables only: it runs on the second stream beside the

@@ -863,6 +863,23 @@ __global__ void k_region_sides(FloodArgs f)
 
 __device__ __forceinline__ bool mixed_region(const FloodArgs &f, int r) { return f.rsMin[r] == 0 && f.rsMax[r] == 1; }
 
+// Level 0 of the flood, grid-wide: flag i (mesh i & 1, entry i >> 1) marks a live entry of a region whose groups
+// were decided differently; anyMixed records whether there is one (usually not: then the flood does nothing).
+__global__ void k_flood_seeds(FloodArgs f)
+{
+    const int nE = 2 * f.info[0], nI = 2 * nE;
+    bool any = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nI; i += gridDim.x * blockDim.x) {
+        const int m = i & 1, q = i >> 1;
+        int t, grp;
+        const int on = (entry_live(f, m * nE + q, nE, t, grp) && mixed_region(f, f.root[t])) ? 1 : 0;
+        f.flag[i] = on;
+        any |= on != 0;
+    }
+    if (__any_sync(0xFFFFFFFFu, any) && (threadIdx.x & 31) == 0)
+        atomicOr(f.anyMixed, 1);
+}
+
 // One block: the reference's first-in-first-out flood (src/solidboolean.cpp:205-233) restricted to the
 // regions whose groups were decided differently, level by level. A level's queue is its triangles in pop
 // order; a triangle first reached at the next level is pushed by the earliest (parent, edge) in that order,
@@ -872,21 +889,12 @@ __global__ void __launch_bounds__(kOrderThreads) k_flood(AsmArgs g, FloodArgs f)
 {
     const int T = blockDim.x, tid = threadIdx.x;
     const int nE = 2 * f.info[0];
-    if (nE == 0)
-        return;
-    __shared__ int nFront;
-    // level 0: live entries of mixed regions, ordered by entry (both meshes interleaved: they never meet)
-    const int nI = 2 * nE;
-    int any = 0;
-    for (int i = tid; i < nI; i += T) {
-        const int m = i & 1, q = i >> 1;
-        int t, grp;
-        const int on = (entry_live(f, m * nE + q, nE, t, grp) && mixed_region(f, f.root[t])) ? 1 : 0;
-        f.flag[i] = on;
-        any |= on;
-    }
-    if (!__syncthreads_or(any))
+    if (nE == 0 || *f.anyMixed == 0)
         return; // every region's groups agree: nothing to flood
+    __shared__ int nFront;
+    // level 0: live entries of mixed regions (flagged by k_flood_seeds), ordered by entry (both meshes
+    // interleaved: they never meet)
+    const int nI = 2 * nE;
     const int n0 = block_excl_scan(f.flag, nI);
     for (int i = tid; i < nI; i += T) {
         const int m = i & 1, q = i >> 1;
@@ -966,6 +974,7 @@ void launch_flood_labels(const AsmArgs &g, const FloodArgs &f, cudaStream_t s)
         return;
     KTime kt("k_flood", s);
     SB_COUNT(k_region_sides)<<<152, 256, 0, s>>>(f);
+    SB_COUNT(k_flood_seeds)<<<152, 256, 0, s>>>(f);
     SB_COUNT(k_flood)<<<1, kOrderThreads, 0, s>>>(g, f);
     SB_COUNT(k_labels_ref)<<<(f.nTri + 255) / 256, 256, 0, s>>>(g, f);
 }

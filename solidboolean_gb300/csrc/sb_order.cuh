@@ -102,7 +102,8 @@ struct FloodArgs {
     const int *insideCount, *regionQuery;
     int *rsMin, *rsMax;  // [nTri] per region: smallest / largest side among its live groups (2 / -1: none)
     int *bfsGroup;       // [nTri] group of each triangle reached by the flood (-1)
-    int *best, *front0, *front1, *tgt, *flag; // scratch: nTri, nTri, nTri, 3 nTri, 3 nTri + 1
+    int *best, *front0, *front1, *tgt, *flag; // scratch: nTri, nTri, nTri, 3 nTri, max(3 nTri, 4 nNew) + 1
+    int *anyMixed;       // [1] set when some region's groups were decided differently (zeroed by the caller)
     unsigned int *errors;
 };
 void launch_flood_labels(const AsmArgs &g, const FloodArgs &f, cudaStream_t s);

@@ -172,50 +172,52 @@ __global__ void k_karras(int n, const uint32_t *__restrict__ code, int2 *__restr
     parent[right >= 0 ? right : (n - 1) + ~right] = i;
 }
 
-__device__ __forceinline__ void load_child_boxes(int c, const int *leafTri, const double *box64, const double *nbox64,
-                                                 const float *nbox32, double *b64, float *b32)
+// Arrival at a node of the climb: an atomic add with acquire-release semantics at device scope. The release
+// publishes the box this thread wrote for the child it climbed from; the acquire makes the sibling's box,
+// written by the thread that arrived first, visible to the loads that follow.
+__device__ __forceinline__ int arrive_acq_rel(int *flag)
 {
-    if (c < 0) {
-        int tri = leafTri[~c];
-        for (int k = 0; k < 6; ++k)
-            b64[k] = __ldcg(box64 + 6 * (size_t)tri + k);
-        for (int k = 0; k < 3; ++k) {
-            b32[k] = __double2float_rd(b64[k]);
-            b32[3 + k] = __double2float_ru(b64[3 + k]);
-        }
-    } else {
-        for (int k = 0; k < 6; ++k) {
-            b64[k] = __ldcg(nbox64 + 6 * (size_t)c + k);
-            b32[k] = __ldcg(nbox32 + 6 * (size_t)c + k);
-        }
-    }
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
+    return old;
 }
 
-// Bottom-up refit: the second thread to reach a node writes the union of its children's boxes.
+// Bottom-up refit: one thread per leaf climbs while it is the second to reach a node, and writes the node's
+// box as the union of the box it carries (its own subtree's, in registers) and the sibling's (one load of six
+// doubles). The FP32 copy rounds the FP64 union outward (down for the low corner, up for the high corner);
+// directed rounding is monotone, so this equals the union of the children's outward-rounded boxes.
 __global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__restrict__ box64,
                         const int2 *__restrict__ child, const int *__restrict__ parent, int *flags, double *nbox64,
                         float *nbox32)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    double m[6];
+    {
+        const int tri = leafTri[i];
+        for (int k = 0; k < 6; ++k)
+            m[k] = box64[6 * (size_t)tri + k];
+    }
+    int cur = ~i; // child id of leaf i
     int node = parent[(n - 1) + i];
     while (node >= 0) {
-        __threadfence();
-        if (atomicAdd(flags + node, 1) == 0)
+        if (arrive_acq_rel(flags + node) == 0)
             return;
-        __threadfence();
-        int2 ch = child[node];
-        double a64[6], b64[6];
-        float a32[6], b32[6];
-        load_child_boxes(ch.x, leafTri, box64, nbox64, nbox32, a64, a32);
-        load_child_boxes(ch.y, leafTri, box64, nbox64, nbox32, b64, b32);
+        const int2 ch = child[node];
+        const int sib = ch.x == cur ? ch.y : ch.x;
+        const double *sb = sib < 0 ? box64 + 6 * (size_t)__ldcg(leafTri + ~sib) : nbox64 + 6 * (size_t)sib;
         for (int k = 0; k < 3; ++k) {
-            nbox64[6 * (size_t)node + k] = fmin(a64[k], b64[k]);
-            nbox64[6 * (size_t)node + 3 + k] = fmax(a64[3 + k], b64[3 + k]);
-            nbox32[6 * (size_t)node + k] = fminf(a32[k], b32[k]);
-            nbox32[6 * (size_t)node + 3 + k] = fmaxf(a32[3 + k], b32[3 + k]);
+            m[k] = fmin(m[k], __ldcg(sb + k));
+            m[3 + k] = fmax(m[3 + k], __ldcg(sb + 3 + k));
         }
+        for (int k = 0; k < 3; ++k) {
+            nbox64[6 * (size_t)node + k] = m[k];
+            nbox64[6 * (size_t)node + 3 + k] = m[3 + k];
+            nbox32[6 * (size_t)node + k] = __double2float_rd(m[k]);
+            nbox32[6 * (size_t)node + 3 + k] = __double2float_ru(m[3 + k]);
+        }
+        cur = node;
         node = parent[node];
     }
 }
