@@ -137,7 +137,10 @@ void DevBuf::release()
     bytes = 0;
 }
 
-static size_t mesh_bytes(int nv, int nt)
+// The prepared arrays of a mesh (the layout prepare_begin carves), then one 256-byte slot for the
+// validation flag, so that creating a mesh allocates nothing else (a temporary buffer that preparation later
+// outgrows would be released, and a release waits for the device).
+static size_t mesh_layout_bytes(int nv, int nt)
 {
     Carve c;
     c.take<double>((size_t)nv * 3);
@@ -157,6 +160,7 @@ static size_t mesh_bytes(int nv, int nt)
     c.take<int>(1);
     return c.off;
 }
+static size_t mesh_bytes(int nv, int nt) { return mesh_layout_bytes(nv, nt) + 256; }
 
 static uint32_t pow2_at_least(size_t n)
 {
@@ -1697,9 +1701,7 @@ static sb_status mesh_validate(sb_mesh *m, cudaStream_t s)
 {
     if (m->d.nt == 0)
         return SB_OK;
-    unsigned int *d_bad = nullptr;
-    SB_CUDA_CHECK(m->tmp.ensure(256));
-    d_bad = m->tmp.as<unsigned int>();
+    unsigned int *d_bad = reinterpret_cast<unsigned int *>(m->buf.as<char>() + mesh_layout_bytes(m->d.nv, m->d.nt));
     SB_CUDA_CHECK(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), s));
     SB_COUNT(k_validate_tris)<<<blocks(3 * (size_t)m->d.nt, 256), 256, 0, s>>>(m->d.nt, m->d.nv, m->d.t, d_bad);
     // the mesh's pinned slot: ints [0, 12) hold the leaf-order status, the last one this flag
