@@ -1037,6 +1037,8 @@ sb_status combine_impl(sb_boolean *b)
         fo.key = (unsigned long long *)(ob + o_fk);
         fo.val = (int *)(ob + o_fv);
         fo.sortedVal = (const int *)(ob + o_fvs);
+        fo.sortedOut = (int *)(ob + o_fvs);
+        fo.blockSort = face_ctx_block_sort(FA, FB) ? 1 : 0;
         fo.faceRank = (int *)(ob + o_fr);
         fo.faceByRank = (int *)(ob + o_fbr);
         fo.insKeys = (uint32_t *)(ob + o_ik);
@@ -1145,10 +1147,11 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
         SB_CUDA_CHECK(cudaStreamWaitEvent(so, b->sideDone, 0));
         launch_face_keys(fo, so);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceRadixSort::SortPairs(tmp, bytes, fo.key, (unsigned long long *)(ob + o_fks), fo.val,
-                                                   (int *)(ob + o_fvs), nFaces, 0, 64, so);
-        }));
+        if (!fo.blockSort) // else k_face_ctx sorts each mesh's faces in its own block
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceRadixSort::SortPairs(tmp, bytes, fo.key, (unsigned long long *)(ob + o_fks), fo.val,
+                                                       (int *)(ob + o_fvs), nFaces, 0, 64, so);
+            }));
         launch_face_ctx(fo, so);
         launch_rank_scan(ra, so);
         SB_CUDA_CHECK(cudaEventRecord(b->orderDone, so));
@@ -1404,7 +1407,6 @@ sb_status combine_impl(sb_boolean *b)
         fl.launch();
     }
     launch_loops(g, s);
-    launch_halfedges(g, s);
     // the loops in the reference's order, the group seeds and each group's first triangle
     const size_t nNewS = (size_t)std::max(nNew, 1), nTriS = (size_t)std::max(nTri, 1);
     const int slotDomain = 4 * (int)K; // first-mesh faces hold 2 K directed cut-edge slots, two sequence slots each
@@ -1488,11 +1490,15 @@ sb_status combine_impl(sb_boolean *b)
         fl.i32(fd.anyMixed, 1, 0);
         fl.launch();
     }
-    // the loop order needs the loop and half-edge tables only: it runs on the second stream beside the
-    // union-find regions, which the side queries need as well
+    // The loop order needs the loop tables only: it runs on the second stream beside the half-edge tables and
+    // the union-find regions; the seeds after it wait for the half-edge tables as well.
     SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s));
     SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
     launch_loop_order(lo, b->side);
+    launch_halfedges(g, s);
+    SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s)); // re-recorded: the wait above already holds the first one
+    SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
+    launch_seed_entries(lo, b->side);
     SB_CUDA_CHECK(cudaEventRecord(b->orderDone, b->side));
     launch_groups(g, s);
     SB_CUDA_CHECK(cudaStreamWaitEvent(s, b->orderDone, 0));

@@ -276,11 +276,54 @@ __global__ void k_face_keys(FaceOrderArgs a)
 }
 
 // one block per mesh: the faces in insertion order (sorted by key) -> iteration order of the context map
+constexpr int kCtxSortMax = 8192; // faces per mesh that k_face_ctx sorts in shared memory
+
+// Bitonic sort of the mesh's faces by (key, face id) in shared memory (n <= kCtxSortMax); writes the face
+// ids in order to out. Keys of one mesh's faces are distinct (distinct first pairs), the id only breaks ties
+// that cannot occur.
+__device__ void face_block_sort(const unsigned long long *key, const int *val, int n, int *out, int *smem)
+{
+    const int T = blockDim.x, tid = threadIdx.x;
+    int N = 1;
+    while (N < n)
+        N <<= 1;
+    unsigned long long *sk = reinterpret_cast<unsigned long long *>(smem);
+    int *sv = reinterpret_cast<int *>(sk + N);
+    for (int i = tid; i < N; i += T) {
+        sk[i] = i < n ? key[i] : ~0ull;
+        sv[i] = i < n ? val[i] : INT_MAX;
+    }
+    __syncthreads();
+    for (int k = 2; k <= N; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < N; i += T) {
+                const int ixj = i ^ j;
+                if (ixj <= i)
+                    continue;
+                const unsigned long long ka = sk[i], kb = sk[ixj];
+                const int va = sv[i], vb = sv[ixj];
+                const bool aAfter = ka > kb || (ka == kb && va > vb);
+                if ((i & k) == 0 ? aAfter : !aAfter) {
+                    sk[i] = kb;
+                    sk[ixj] = ka;
+                    sv[i] = vb;
+                    sv[ixj] = va;
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = tid; i < n; i += T)
+        out[i] = sv[i];
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(kOrderThreads) k_face_ctx(FaceOrderArgs a, int smemInts)
 {
     extern __shared__ __align__(16) int dsm[];
     const int side = blockIdx.x;
     const int off = side ? a.FA : 0, n = side ? a.FB : a.FA;
+    if (a.blockSort)
+        face_block_sort(a.key + off, a.val + off, n, a.sortedOut + off, dsm);
     uint32_t *keys = a.insKeys + off;
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         keys[i] = (uint32_t)a.faceTri[a.sortedVal[off + i]];
@@ -321,17 +364,28 @@ void launch_face_keys(const FaceOrderArgs &a, cudaStream_t s)
 }
 
 constexpr int kFaceCtxSmemBytes = 226 * 1024; // of the 227 KB a block may take, leaving room for static arrays
+static_assert(kCtxSortMax * (sizeof(unsigned long long) + sizeof(int)) <= kFaceCtxSmemBytes, "sort fits");
 
-void launch_face_ctx(const FaceOrderArgs &a, cudaStream_t s)
+static int face_ctx_smem_bytes()
 {
-    if (a.nFaces <= 0)
-        return;
     static std::once_flag once;
     static cudaError_t attrErr = cudaSuccess;
     std::call_once(once, [] {
         attrErr = cudaFuncSetAttribute(k_face_ctx, cudaFuncAttributeMaxDynamicSharedMemorySize, kFaceCtxSmemBytes);
     });
-    const int bytes = attrErr == cudaSuccess ? kFaceCtxSmemBytes : 0;
+    return attrErr == cudaSuccess ? kFaceCtxSmemBytes : 0;
+}
+
+bool face_ctx_block_sort(int FA, int FB)
+{
+    return std::max(FA, FB) <= kCtxSortMax && face_ctx_smem_bytes() > 0;
+}
+
+void launch_face_ctx(const FaceOrderArgs &a, cudaStream_t s)
+{
+    if (a.nFaces <= 0)
+        return;
+    const int bytes = face_ctx_smem_bytes();
     KTime kt("k_face_order", s);
     SB_COUNT(k_face_ctx)<<<2, kOrderThreads, bytes, s>>>(a, bytes / 4);
 }
@@ -804,10 +858,12 @@ void launch_loop_order(LoopOrderArgs a, cudaStream_t s)
         attrErr = cudaFuncSetAttribute(k_loop_order, cudaFuncAttributeMaxDynamicSharedMemorySize, kOrderSmemBytes);
     });
     a.smemInts = attrErr == cudaSuccess ? kOrderSmemBytes / 4 : 0;
-    {
-        KTime kt("k_loop_order", s);
-        SB_COUNT(k_loop_order)<<<1, kOrderThreads, attrErr == cudaSuccess ? kOrderSmemBytes : 0, s>>>(a);
-    }
+    KTime kt("k_loop_order", s);
+    SB_COUNT(k_loop_order)<<<1, kOrderThreads, attrErr == cudaSuccess ? kOrderSmemBytes : 0, s>>>(a);
+}
+
+void launch_seed_entries(const LoopOrderArgs &a, cudaStream_t s)
+{
     const int n = std::max(a.nNew, 1);
     KTime kt("k_seed_entries", s);
     SB_COUNT(k_seed_entries)<<<(n + 255) / 256, 256, 0, s>>>(a);

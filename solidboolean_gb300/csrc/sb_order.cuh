@@ -34,6 +34,8 @@ struct FaceOrderArgs {
     unsigned long long *key;   // [nFaces] traversal key of each face's first pair
     int *val;                  // [nFaces] face ids
     const int *sortedVal;      // [nFaces] faces sorted by key (mesh first)
+    int *sortedOut;            // the same array, written by k_face_ctx when it sorts (blockSort)
+    int blockSort;             // k_face_ctx sorts each mesh's faces by key itself (face_ctx_block_sort)
     int *faceRank;             // [nFaces] position in the reference's processing order (first mesh first)
     int *faceByRank;           // [nFaces]
     uint32_t *insKeys;         // [nFaces] scratch
@@ -44,6 +46,9 @@ struct FaceOrderArgs {
 void launch_face_keys(const FaceOrderArgs &a, cudaStream_t s);
 // faces sorted by key -> context-map iteration order per mesh (k_face_ctx)
 void launch_face_ctx(const FaceOrderArgs &a, cudaStream_t s);
+// whether k_face_ctx can sort each mesh's faces by key in its own block (up to 8,192 faces per mesh); else
+// the caller sorts them device-wide into sortedVal first
+bool face_ctx_block_sort(int FA, int FB);
 
 // Exclusive scans of per-face values taken in the processing order: out[f] = sum of vals over the faces
 // ranked before f; tot[0] = sum over the first mesh's faces, tot[1] = sum over all. Up to three arrays.
@@ -88,8 +93,10 @@ struct LoopOrderArgs {
     unsigned long long *stamps; // [8] device time at the phase boundaries (diagnostics; may be null)
 };
 size_t loop_order_scratch_ints(int slotDomain, int nNew);
-// the loop order (one block), the seed entries and each group's first entry (grid-wide)
+// the loop order (one block); it needs the loop tables only
 void launch_loop_order(LoopOrderArgs a, cudaStream_t s);
+// the seed entries and each group's first entry (grid-wide); they need the loop order and the half-edge tables
+void launch_seed_entries(const LoopOrderArgs &a, cudaStream_t s);
 // side queries of the groups and of the regions without seeds (needs the union-find regions)
 void launch_side_queries(const AsmArgs &g, const LoopOrderArgs &a, cudaStream_t s);
 

@@ -983,7 +983,7 @@ __device__ void create_children(int id, RNode *nodes, NParam *np, int *counters,
     __syncthreads(); // sBase is reused by the next node of this block
 }
 
-__global__ void __launch_bounds__(kElemThreads, 4)
+__global__ void __launch_bounds__(kElemThreads, 3)
     k_rr_top(int nt, const RRec *__restrict__ rec, const unsigned long long *__restrict__ soa, int *state, NParam *np,
              RNode *nodes, int *counters, int *terms,
              int maxNodes, const int *__restrict__ posOf, int *pool, const int *__restrict__ scg, GridBar *gb,

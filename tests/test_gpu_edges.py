@@ -157,3 +157,28 @@ def test_device_earcut_random_polygons(gpu_lib):
     for p in range(len(po) - 1):
         rings = [xy[ro[r]:ro[r + 1]] for r in range(po[p], po[p + 1])]
         assert np.array_equal(_earcut(gpu_lib, rings), idx[io[p]:io[p + 1]]), p
+
+
+def test_out_of_range_triangle_is_rejected(gpu_lib):
+    """A triangle index at or past the vertex count is an argument error (SB_ERR_INVALID), from the host and
+    the device variant alike; nothing is left allocated or pending."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    L = sbg.lib()
+    v, f = mg.icosphere(1)
+    bad = np.ascontiguousarray(f, dtype=np.uint32).copy()
+    bad[7, 1] = len(v)  # one past the last vertex
+    v = np.ascontiguousarray(v)
+    h = ctypes.c_void_p()
+    assert L.sb_mesh_create(v.ctypes.data, len(v), bad.ctypes.data, len(bad), ctypes.byref(h)) == sbg.SB_ERR_INVALID
+    assert not h.value
+    dv = torch.from_numpy(v).cuda()
+    dt = torch.from_numpy(bad.astype(np.int32)).cuda()
+    opts = sbg.make_options()
+    assert L.sb_mesh_create_device(dv.data_ptr(), len(v), dt.data_ptr(), len(bad), ctypes.byref(opts),
+                                   ctypes.byref(h)) == sbg.SB_ERR_INVALID
+    assert not h.value
+    # a valid mesh still works afterwards
+    good = np.ascontiguousarray(f, dtype=np.uint32)
+    assert L.sb_mesh_create(v.ctypes.data, len(v), good.ctypes.data, len(good), ctypes.byref(h)) == sbg.SB_OK
+    L.sb_mesh_destroy(h)
