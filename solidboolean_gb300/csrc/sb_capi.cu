@@ -158,6 +158,7 @@ static size_t mesh_layout_bytes(int nv, int nt)
     c.take<int>((size_t)nt);
     c.take<int>((size_t)nt * 3);
     c.take<int>(1);
+    c.take<float4>((size_t)(nt > 1 ? nt - 1 : 1) * 4);
     return c.off;
 }
 static size_t mesh_bytes(int nv, int nt) { return mesh_layout_bytes(nv, nt) + 256; }
@@ -992,23 +993,29 @@ sb_status combine_impl(sb_boolean *b)
     char *ob = nullptr;
     size_t o_fks = 0, o_fvs = 0;
     if (nFaces > 0) {
-        SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
-        }));
-        launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s);
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, scratchBytes, scratchOff, nFaces + 1, s);
-        }));
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, ptCap, ptOff, nFaces + 1, s);
-        }));
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, triCapA, triOff, nFaces + 1, s);
-        }));
-        SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-            return cub::DeviceScan::ExclusiveSum(tmp, bytes, edgeCap, edgeOff, nFaces + 1, s);
-        }));
+        if (nFaces <= kFaceLayoutBlockMax) {
+            launch_face_layout(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri, faceCnt, faceBegin, scratchOff, ptCap,
+                               ptOff, triCapA, triOff, edgeCap, edgeOff, s);
+        } else {
+            SB_COUNT(k_face_table)<<<blocks(nFaces, 256), 256, 0, s>>>(FA, FB, uqA, ctA, uqB, ctB, faceSide, faceTri,
+                                                                       faceCnt);
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, faceCnt, faceBegin, nFaces + 1, s);
+            }));
+            launch_face_sizes(nFaces, faceBegin, scratchBytes, ptCap, triCapA, edgeCap, s);
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, scratchBytes, scratchOff, nFaces + 1, s);
+            }));
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, ptCap, ptOff, nFaces + 1, s);
+            }));
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, triCapA, triOff, nFaces + 1, s);
+            }));
+            SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
+                return cub::DeviceScan::ExclusiveSum(tmp, bytes, edgeCap, edgeOff, nFaces + 1, s);
+            }));
+        }
         // the reference's processing order of the cut faces: each face keyed by its first pair's place in the
         // tree traversal, sorted, then ordered like the context map iterates them
         Carve co;

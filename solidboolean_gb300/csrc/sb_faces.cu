@@ -647,6 +647,89 @@ __global__ void __launch_bounds__(32) k_faces(FaceArgs a)
     a.faceNedges[f] = r.status == 0 ? r.nedges : 0;
 }
 
+// Exclusive scan of n + 1 values in place by one block (a[n] receives the total); every thread must call it.
+template <class T> __device__ T block_scan_inplace(T *a, int n)
+{
+    __shared__ T part[32];
+    __shared__ T carry;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, W = blockDim.x >> 5;
+    if (tid == 0)
+        carry = 0;
+    __syncthreads();
+    for (int base = 0; base <= n; base += blockDim.x) {
+        const int i = base + tid;
+        const T x = i < n ? a[i] : T(0);
+        T y = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const T v = __shfl_up_sync(0xFFFFFFFFu, y, o);
+            if (lane >= o)
+                y += v;
+        }
+        if (lane == 31)
+            part[w] = y;
+        __syncthreads();
+        if (w == 0) {
+            T z = lane < W ? part[lane] : T(0);
+            for (int o = 1; o < 32; o <<= 1) {
+                const T v = __shfl_up_sync(0xFFFFFFFFu, z, o);
+                if (lane >= o)
+                    z += v;
+            }
+            part[lane] = z; // inclusive over warps
+        }
+        __syncthreads();
+        const T before = carry + (w > 0 ? part[w - 1] : T(0)) + (y - x);
+        if (i <= n)
+            a[i] = before;
+        __syncthreads();
+        if (tid == 0)
+            carry += part[W - 1];
+        __syncthreads();
+    }
+    return carry;
+}
+
+// The cut faces' table and buffer layout in one launch (one block; for up to kFaceLayoutBlockMax faces): side,
+// triangle and pair count of each face, its first pair (exclusive scan of the counts) and the exclusive scans
+// of its scratch bytes and point, triangle and edge capacities, each with its total in entry nFaces.
+__global__ void __launch_bounds__(1024) k_face_layout(int FA, int FB, const int *__restrict__ uniqA,
+                                                      const int *__restrict__ cntA, const int *__restrict__ uniqB,
+                                                      const int *__restrict__ cntB, int *faceSide, int *faceTri,
+                                                      int *faceCnt, int *faceBegin, unsigned long long *scratchOff,
+                                                      int *ptCap, int *ptOff, int *triCap, int *triOff,
+                                                      int *edgeCap, int *edgeOff)
+{
+    const int n = FA + FB;
+    for (int f = threadIdx.x; f < n; f += blockDim.x) {
+        const bool a = f < FA;
+        const int np = a ? cntA[f] : cntB[f - FA];
+        faceSide[f] = a ? 0 : 1;
+        faceTri[f] = a ? uniqA[f] : uniqB[f - FA];
+        faceCnt[f] = np;
+        faceBegin[f] = np;
+        scratchOff[f] = (unsigned long long)face_scratch_bytes_dev(np);
+        ptCap[f] = ptOff[f] = 2 * np;
+        triCap[f] = triOff[f] = 32 * np + 16;
+        edgeCap[f] = edgeOff[f] = 2 * np; // directed: each undirected edge from both ends
+    }
+    __syncthreads();
+    block_scan_inplace(faceBegin, n);
+    block_scan_inplace(scratchOff, n);
+    block_scan_inplace(ptOff, n);
+    block_scan_inplace(triOff, n);
+    block_scan_inplace(edgeOff, n);
+}
+
+void launch_face_layout(int FA, int FB, const int *uniqA, const int *cntA, const int *uniqB, const int *cntB,
+                        int *faceSide, int *faceTri, int *faceCnt, int *faceBegin, unsigned long long *scratchOff,
+                        int *ptCap, int *ptOff, int *triCap, int *triOff, int *edgeCap, int *edgeOff, cudaStream_t s)
+{
+    if (FA + FB <= 0)
+        return;
+    SB_COUNT(k_face_layout)<<<1, 1024, 0, s>>>(FA, FB, uniqA, cntA, uniqB, cntB, faceSide, faceTri, faceCnt, faceBegin,
+                                               scratchOff, ptCap, ptOff, triCap, triOff, edgeCap, edgeOff);
+}
+
 // per-face capacities: scratch bytes, points, triangles, edges (written as counts; scanned by the caller)
 __global__ void k_face_sizes(int nFaces, const int *__restrict__ faceBegin, unsigned long long *scratchBytes,
                              int *ptCap, int *triCap, int *edgeCap)

@@ -33,5 +33,11 @@ size_t face_scratch_bytes_host(int np);
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
                        int *edgeCap, cudaStream_t s);
 void launch_faces(const FaceArgs &a, cudaStream_t s);
+// The cut faces' table, first pairs and buffer offsets (exclusive scans with the totals in entry FA + FB) in
+// one launch of one block, for up to kFaceLayoutBlockMax faces; past that the caller scans device-wide.
+constexpr int kFaceLayoutBlockMax = 1 << 16;
+void launch_face_layout(int FA, int FB, const int *uniqA, const int *cntA, const int *uniqB, const int *cntB,
+                        int *faceSide, int *faceTri, int *faceCnt, int *faceBegin, unsigned long long *scratchOff,
+                        int *ptCap, int *ptOff, int *triCap, int *triOff, int *edgeCap, int *edgeOff, cudaStream_t s);
 
 } // namespace sbg
