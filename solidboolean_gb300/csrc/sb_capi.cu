@@ -158,7 +158,6 @@ static size_t mesh_layout_bytes(int nv, int nt)
     c.take<int>((size_t)nt);
     c.take<int>((size_t)nt * 3);
     c.take<int>(1);
-    c.take<float4>((size_t)(nt > 1 ? nt - 1 : 1) * 4);
     return c.off;
 }
 static size_t mesh_bytes(int nv, int nt) { return mesh_layout_bytes(nv, nt) + 256; }
@@ -1075,18 +1074,14 @@ sb_status combine_impl(sb_boolean *b)
         ra.tmp[1] = rankTmp[1];
         ra.tot[0] = rankTot;
         ra.tot[1] = rankTot + 2;
-        unsigned long long sTot = 0;
-        int pTot = 0, tTot = 0, eTot = 0;
-        Readback rb(b);
-        SB_CUDA_CHECK(rb.add(&sTot, scratchOff + nFaces, sizeof sTot));
-        SB_CUDA_CHECK(rb.add(&pTot, ptOff + nFaces, sizeof pTot));
-        SB_CUDA_CHECK(rb.add(&tTot, triOff + nFaces, sizeof tTot));
-        SB_CUDA_CHECK(rb.add(&eTot, edgeOff + nFaces, sizeof eTot));
-        SB_CUDA_CHECK(rb.sync());
-        totals[0] = (long long)sTot;
-        totals[1] = pTot;
-        totals[2] = tTot;
-        totals[3] = eTot;
+        // The totals follow from the pair count without a read-back: every intersecting pair cuts one face of
+        // each mesh, so the faces' pair counts sum to 2 K; a face of np pairs takes 2 np points, 2 np directed
+        // edges and 32 np + 16 triangles. Its scratch is bounded by an affine function of np
+        // (face_scratch_bound); the re-triangulation checks the bound per face.
+        totals[0] = (long long)face_scratch_bound(nFaces, 2 * (long long)K);
+        totals[1] = 4 * (long long)K;
+        totals[2] = 64 * (long long)K + 16 * (long long)nFaces;
+        totals[3] = 4 * (long long)K;
     }
     AsmArgs g;
     std::memset(&g, 0, sizeof g);
@@ -1201,6 +1196,7 @@ sb_status combine_impl(sb_boolean *b)
         fa.faceNedges = faceNedges;
         fa.ptSrc = ptSrc;
         fa.robustEdges = (b->opts.robust & SB_ROBUST_EDGE_TOLERANCE) != 0;
+        fa.scratchCap = (unsigned long long)totals[0];
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }

@@ -132,6 +132,22 @@ __host__ __device__ inline size_t face_carve(int np, char *base, FacePtrs *p)
 }
 
 size_t face_scratch_bytes_host(int np) { return face_carve(np, nullptr, nullptr); }
+
+size_t face_scratch_bound(long long nFaces, long long sumNp)
+{
+    static const size_t alpha = face_scratch_bytes_host(1);
+    static const size_t beta = [] {
+        size_t b = 0;
+        for (int np = 2; np <= 65536; ++np) {
+            const size_t x = face_scratch_bytes_host(np), d = x > alpha ? x - alpha : 0;
+            b = std::max(b, (d + (size_t)np - 2) / (size_t)(np - 1));
+        }
+        return b;
+    }();
+    if (nFaces <= 0)
+        return 0;
+    return alpha * (size_t)nFaces + beta * (size_t)std::max(0ll, sumNp - nFaces);
+}
 __device__ size_t face_scratch_bytes_dev(int np) { return face_carve(np, nullptr, nullptr); }
 
 // Orders the distinct keys keys[0..n) like the library does (hash_iteration_order), writing the keys
@@ -640,6 +656,11 @@ __global__ void __launch_bounds__(32) k_faces(FaceArgs a)
     job.tri = a.faceTri[f];
     job.pairBegin = a.faceBegin[f];
     job.pairEnd = a.faceBegin[f + 1];
+    if (a.scratchOff[f + 1] > a.scratchCap) { // past the allocation's bound (never expected): capacity
+        a.faceStatus[f] = 3;
+        a.faceNpts[f] = a.faceNtris[f] = a.faceNedges[f] = 0;
+        return;
+    }
     FaceOut r = process_face(job, a, f, a.scratch + a.scratchOff[f]);
     a.faceStatus[f] = r.status;
     a.faceNpts[f] = r.npts;

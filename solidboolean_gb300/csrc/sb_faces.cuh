@@ -27,9 +27,14 @@ struct FaceArgs {
     int *faceStatus, *faceNpts, *faceNtris, *faceNedges;
     int *ptSrc = nullptr; // optional, per face point: 2 x (intersecting pair) + segment end it came from
     int robustEdges = 0;  // SB_ROBUST_EDGE_TOLERANCE: scale-relative point-on-edge test (0: the reference's)
+    unsigned long long scratchCap = ~0ull; // bytes of scratch; a face whose slice ends past it reports capacity
 };
 
 size_t face_scratch_bytes_host(int np);
+// An upper bound of the summed scratch of nFaces faces whose pair counts sum to sumNp, each of at most 65,536
+// pairs: alpha nFaces + beta (sumNp - nFaces) with alpha the scratch of one pair and beta the largest increment
+// per further pair (computed once).
+size_t face_scratch_bound(long long nFaces, long long sumNp);
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
                        int *edgeCap, cudaStream_t s);
 void launch_faces(const FaceArgs &a, cudaStream_t s);

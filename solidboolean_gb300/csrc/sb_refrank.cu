@@ -935,25 +935,24 @@ __device__ void resolve_node(int id, int nt, const RRec *__restrict__ rec, int *
     __syncthreads();
 }
 
-// The children of one split node, one thread each (threads 0 and 1; all threads of the block call it): ids
+// The children of one split node, by one warp (lanes 0 and 1 write one child each; all 32 lanes call it): ids
 // and terminal-list slots from atomic counters (node ids carry no order; begin offsets and direction bits
 // do), statistics and split parameters.
 __device__ void create_children(int id, RNode *nodes, NParam *np, int *counters, int *terms, int maxNodes,
-                                const int *sc, int *sBase)
+                                const int *sc)
 {
     RNode &nd = nodes[id];
-    if (threadIdx.x == 0) {
-        const int c = atomicAdd(counters + kCtNodes, 2);
+    const int lane = threadIdx.x & 31;
+    int c = 0;
+    if (lane == 0) {
+        c = atomicAdd(counters + kCtNodes, 2);
         if (c + 2 > maxNodes) {
             atomicExch(counters + kCtOverflow, 1); // nothing is split further; the host reports the overflow
-            *sBase = -1;
-        } else {
-            *sBase = c;
+            c = -1;
         }
     }
-    __syncthreads();
-    const int c = *sBase;
-    const int s2 = threadIdx.x;
+    c = __shfl_sync(0xFFFFFFFFu, c, 0);
+    const int s2 = lane;
     if (c >= 0 && s2 < 2) {
         const RStat acc = ld_rstat(&nd.acc[s2]);
         const int leftCount = __ldcg(&nd.acc[0].count);
@@ -980,7 +979,6 @@ __device__ void create_children(int id, RNode *nodes, NParam *np, int *counters,
         if (s2 == 0)
             np[id].child = c; // read only after the grid barrier that ends this phase
     }
-    __syncthreads(); // sBase is reused by the next node of this block
 }
 
 __global__ void __launch_bounds__(kElemThreads, 3)
@@ -1020,6 +1018,8 @@ __global__ void __launch_bounds__(kElemThreads, 3)
         if (!grid_sync(gb))
             return;
         stamp(level, 1);
+        // the block's nodes: the rare exact resolutions first (whole block each), then the children, one
+        // warp per node
         for (int id = first + blockIdx.x; id < last; id += gridDim.x) {
             RNode &nd = nodes[id];
             const int count = __ldcg(&nd.count);
@@ -1030,7 +1030,14 @@ __global__ void __launch_bounds__(kElemThreads, 3)
             if (flagged) // members of one level's nodes are disjoint: the node's leaf range is its list space
                 resolve_node(id, nt, rec, state, ld_nparam(&np[id]), nd, pool + __ldcg(&nd.begin), posOf, warpRuns,
                              runs, sAcc, sLeft, sSplit, reinterpret_cast<double *>(tab.par));
-            create_children(id, nodes, np, counters, terms, maxNodes, sc, &sLeft);
+        }
+        __syncthreads();
+        {
+            const int w = threadIdx.x >> 5, W = blockDim.x >> 5;
+            int k = 0;
+            for (int id = first + blockIdx.x; id < last; id += gridDim.x, ++k)
+                if (k % W == w && __ldcg(&nodes[id].count) > kSub)
+                    create_children(id, nodes, np, counters, terms, maxNodes, sc);
         }
         if (!grid_sync(gb))
             return;
