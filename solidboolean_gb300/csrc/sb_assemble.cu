@@ -350,9 +350,11 @@ __global__ void k_union_adj(int nTri, int uncutA, int uncutB, const uint32_t *__
             const int j = M.adj[3 * (size_t)i + k];
             if (j < 0)
                 continue;
+            // two uncut neighbours see each other (every directed edge is held once, so the adjacency is
+            // symmetric): the edge is joined from its higher end only
             const int tw = !cut[j] ? outBase + urank[j]
                                    : u64map_find(keys, vals, mask, he_key(v[(k + 1) % 3], v[k]));
-            if (tw >= 0)
+            if (tw >= 0 && (cut[j] || tw < t))
                 uf_union(parent, t, tw);
         }
     } else {

@@ -173,6 +173,7 @@ extern "C" sb_status sb_retriangulate_faces_noalloc(const double *d_corners, con
     }
     FaceArgs fa;
     std::memset(&fa, 0, sizeof fa);
+    fa.scratchCap = ~0ull; // the workspace total was checked against the static array above
     fa.A.v = const_cast<double *>(d_corners);
     fa.A.nv = 3 * n_faces;
     fa.A.t = cornerTris;
