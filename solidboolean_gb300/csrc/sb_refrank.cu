@@ -732,25 +732,36 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
                 state[p] = nv;
         }
         int len = key >= 0 ? 1 : 0;
-        // the usual case in Morton order: the whole chunk holds one key (or none). Its totals join the carried
-        // run when the key continues it, else the carried run is flushed and this chunk opens the next one;
-        // a chunk without keys leaves the carried run open (runs of one key merge in any grouping).
+        // the usual case in Morton order: the whole chunk holds one key (or none). The carried run is kept as
+        // one partial per lane while chunks continue it, each lane adding its own member (no warp reduction);
+        // it is summed across the warp only when it ends. A chunk without keys leaves the carried run open
+        // (runs of one key merge in any grouping).
         const int key0 = __shfl_sync(full, key, 0);
         if (__all_sync(full, key == key0)) {
             if (key0 < 0)
                 continue;
-            warp_uniform_reduce(e, len);
             if (openKey == key0) {
                 estat_merge(open, e);
                 openLen += len;
             } else {
-                if (openKey >= 0 && lane == 0)
-                    stat_atomic(target(openKey), open, openLen);
+                if (openKey >= 0) {
+                    warp_uniform_reduce(open, openLen);
+                    if (lane == 0)
+                        stat_atomic(target(openKey), open, openLen);
+                }
                 openKey = key0;
                 openLen = len;
                 open = e;
             }
             continue;
+        }
+        // a chunk of several keys: the carried run's partials are summed into lane 0 first
+        if (openKey >= 0) {
+            warp_uniform_reduce(open, openLen);
+            if (lane != 0) {
+                estat_neutral(open);
+                openLen = 0;
+            }
         }
         // the carried run continues into lane 0 or is complete
         if (lane == 0) {
@@ -785,11 +796,17 @@ __device__ __forceinline__ void classify_range(int wb, int we, int prevFirst, in
             e31.hi[k] = __shfl_sync(full, e.hi[k], 31);
             e31.s[k] = __shfl_sync(full, e.s[k], 31);
         }
+        // the run through lane 31 stays open, held by lane 0 (the other lanes' partials start empty)
         openKey = k31;
-        openLen = l31;
-        open = e31;
+        openLen = lane == 0 ? l31 : 0;
+        if (lane == 0)
+            open = e31;
+        else
+            estat_neutral(open);
     }
-    // lane 0 holds the open run; it joins the block reduction
+    // the open run's partials summed into lane 0; it joins the block reduction
+    if (openKey >= 0)
+        warp_uniform_reduce(open, openLen);
     const int fk = lane == 0 ? openKey : -1;
     block_reduce_keys(fk, open, lane == 0 ? openLen : 0, runs, warpRuns, target);
 }
