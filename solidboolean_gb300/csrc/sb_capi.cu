@@ -973,6 +973,7 @@ sb_status combine_impl(sb_boolean *b)
     size_t o_po = cf.take<int>(nFaces + 1), o_to = cf.take<int>(nFaces + 1), o_eo = cf.take<int>(nFaces + 1);
     size_t o_fst = cf.take<int>(nFaces + 1), o_fnp = cf.take<int>(nFaces + 1), o_fnt = cf.take<int>(nFaces + 1);
     size_t o_fne = cf.take<int>(nFaces + 1), o_rr = cf.take<int>(nFaces + 1);
+    size_t o_frm = cf.take<double>(6 * ((size_t)nFaces + 1));
     SB_CUDA_CHECK(b->faces.ensure(cf.off));
     char *fb = b->faces.as<char>();
     int *faceSide = (int *)(fb + o_side), *faceTri = (int *)(fb + o_tri), *faceCnt = (int *)(fb + o_cnt);
@@ -982,6 +983,7 @@ sb_status combine_impl(sb_boolean *b)
     int *ptOff = (int *)(fb + o_po), *triOff = (int *)(fb + o_to), *edgeOff = (int *)(fb + o_eo);
     int *faceStatus = (int *)(fb + o_fst), *faceNpts = (int *)(fb + o_fnp), *faceNtris = (int *)(fb + o_fnt);
     int *faceNedges = (int *)(fb + o_fne), *retriRank = (int *)(fb + o_rr);
+    double *faceFrames = (double *)(fb + o_frm);
     SB_CUDA_CHECK(cudaMemsetAsync(fb, 0, cf.off, s));
     long long totals[4] = {0, 0, 0, 0};
     int *faceRank = nullptr, *faceByRank = nullptr, *ptRef = nullptr, *edgeRef = nullptr, *retriRef = nullptr;
@@ -1015,6 +1017,7 @@ sb_status combine_impl(sb_boolean *b)
                 return cub::DeviceScan::ExclusiveSum(tmp, bytes, edgeCap, edgeOff, nFaces + 1, s);
             }));
         }
+        launch_face_frames(nFaces, faceSide, faceTri, A, B, faceFrames, s); // needs no leaf order
         // the reference's processing order of the cut faces: each face keyed by its first pair's place in the
         // tree traversal, sorted, then ordered like the context map iterates them
         Carve co;
@@ -1197,6 +1200,7 @@ sb_status combine_impl(sb_boolean *b)
         fa.ptSrc = ptSrc;
         fa.robustEdges = (b->opts.robust & SB_ROBUST_EDGE_TOLERANCE) != 0;
         fa.scratchCap = (unsigned long long)totals[0];
+        fa.frames = faceFrames;
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }

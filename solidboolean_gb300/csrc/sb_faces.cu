@@ -194,6 +194,49 @@ struct FaceOut {
     int status, npts, ntris, nedges;
 };
 
+// The projection frame of a face (ReTriangulator's constructor, src/retriangulator.cpp:29-37): the axis along
+// its first edge and the in-plane perpendicular cross(normal, axis).
+SB_HDF void face_frame(const d3 *c, d3 &axis, d3 &perp)
+{
+    const d3 normal = unit_normal(c[0], c[1], c[2]);
+    axis = normalized(c[1] - c[0]);
+    perp = cross(normal, axis);
+}
+
+// One thread per face, so that the divisions and square roots of the frames run with the warps' lanes
+// converged (inside the re-triangulation two faces share a warp and the FP64 pipe issues whole warps).
+__global__ void k_face_frames(int nFaces, const int *__restrict__ faceSide, const int *__restrict__ faceTri,
+                              MeshDev A, MeshDev B, double *frames)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nFaces)
+        return;
+    const MeshDev &M = faceSide[f] == 0 ? A : B;
+    const int tri = faceTri[f];
+    d3 c[3];
+    for (int k = 0; k < 3; ++k) {
+        const double *p = M.v + 3 * (size_t)M.t[3 * (size_t)tri + k];
+        c[k] = mk(p[0], p[1], p[2]);
+    }
+    d3 axis, perp;
+    face_frame(c, axis, perp);
+    double *fr = frames + 6 * (size_t)f;
+    fr[0] = axis.x;
+    fr[1] = axis.y;
+    fr[2] = axis.z;
+    fr[3] = perp.x;
+    fr[4] = perp.y;
+    fr[5] = perp.z;
+}
+
+void launch_face_frames(int nFaces, const int *faceSide, const int *faceTri, const MeshDev &A, const MeshDev &B,
+                        double *frames, cudaStream_t s)
+{
+    if (nFaces <= 0)
+        return;
+    SB_COUNT(k_face_frames)<<<(nFaces + 31) / 32, 32, 0, s>>>(nFaces, faceSide, faceTri, A, B, frames);
+}
+
 SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *scratchBase)
 {
     FaceOut res{0, 0, 0, 0};
@@ -300,9 +343,14 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
     double faceScale = 0.0; // largest absolute corner coordinate (the robust point-on-edge bound)
     for (int k = 0; k < 3; ++k)
         faceScale = fmax(faceScale, fmax(fabs(c[k].x), fmax(fabs(c[k].y), fabs(c[k].z))));
-    d3 normal = unit_normal(c[0], c[1], c[2]);
-    d3 axis = normalized(c[1] - c[0]);
-    d3 perp = cross(normal, axis);
+    d3 axis, perp;
+    if (a.frames) { // computed beforehand by k_face_frames, with the same operations
+        const double *fr = a.frames + 6 * (size_t)f;
+        axis = mk(fr[0], fr[1], fr[2]);
+        perp = mk(fr[3], fr[4], fr[5]);
+    } else {
+        face_frame(c, axis, perp);
+    }
     for (int k = 0; k < 3; ++k) {
         d3 dir = c[k] - c[0];
         s.pts2[k] = d2{dot(dir, axis), dot(dir, perp)};

@@ -28,6 +28,7 @@ struct FaceArgs {
     int *ptSrc = nullptr; // optional, per face point: 2 x (intersecting pair) + segment end it came from
     int robustEdges = 0;  // SB_ROBUST_EDGE_TOLERANCE: scale-relative point-on-edge test (0: the reference's)
     unsigned long long scratchCap = ~0ull; // bytes of scratch; a face whose slice ends past it reports capacity
+    const double *frames = nullptr;        // optional: per face its projection axis and perpendicular (6 doubles)
 };
 
 size_t face_scratch_bytes_host(int np);
@@ -38,6 +39,9 @@ size_t face_scratch_bound(long long nFaces, long long sumNp);
 void launch_face_sizes(int nFaces, const int *faceBegin, unsigned long long *scratchBytes, int *ptCap, int *triCap,
                        int *edgeCap, cudaStream_t s);
 void launch_faces(const FaceArgs &a, cudaStream_t s);
+// per face the projection axis and perpendicular, one thread per face (FaceArgs::frames)
+void launch_face_frames(int nFaces, const int *faceSide, const int *faceTri, const MeshDev &A, const MeshDev &B,
+                        double *frames, cudaStream_t s);
 // The cut faces' table, first pairs and buffer offsets (exclusive scans with the totals in entry FA + FB) in
 // one launch of one block, for up to kFaceLayoutBlockMax faces; past that the caller scans device-wide.
 constexpr int kFaceLayoutBlockMax = 1 << 16;
