@@ -1201,6 +1201,7 @@ sb_status combine_impl(sb_boolean *b)
         fa.robustEdges = (b->opts.robust & SB_ROBUST_EDGE_TOLERANCE) != 0;
         fa.scratchCap = (unsigned long long)totals[0];
         fa.frames = faceFrames;
+        fa.filteredEarcut = fp64 ? 0 : 1;
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
     }

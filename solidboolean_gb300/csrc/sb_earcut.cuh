@@ -20,6 +20,7 @@ SB_HD double smax(double a, double b) { return (a < b) ? b : a; }
 
 struct EcNode {
     double x, y;
+    float xf, yf; // round-to-nearest FP32 copies for the filtered orientation tests
     int i;
     int prev, next;
     int z;
@@ -40,6 +41,15 @@ struct DevEarcut {
     double minX = 0, minY = 0, maxX = 0, maxY = 0, invSize = 0;
     int error = 0; // 1 = capacity, 2 = iteration budget
     long long budget = 0;
+    // Filtered orientation tests. Every orientation below is a difference of two products of coordinate
+    // differences. Evaluated in FP32 on the FP32 copies, its error against the exact value is at most
+    // 48.5 * 2^-24 * M^2 (M: the largest absolute coordinate; input rounding, three roundings per product
+    // chain and the final subtraction), and the reference's FP64 evaluation is within 40 * 2^-53 * M^2 of the
+    // exact value. So when the FP32 value exceeds 2^-17 M^2 plus a constant that covers the FP64 error (and,
+    // for area(), the DBL_EPSILON snap), the FP64 result has the FP32 value's sign and is not snapped; else
+    // the FP64 expression is evaluated as the reference does.
+    float cmax = 0.f, thrArea = 0x1p-50f, thrOrient = 0x1p-60f;
+    bool filtered = true; // false: every orientation in FP64 (the plain FP64 form)
 
     SB_HD bool tick()
     {
@@ -59,6 +69,12 @@ struct DevEarcut {
         EcNode &n = N[cnt];
         n.x = x;
         n.y = y;
+        n.xf = (float)x;
+        n.yf = (float)y;
+        cmax = fmaxf(cmax, fmaxf(fabsf(n.xf), fabsf(n.yf))); // (a NaN coordinate is skipped: its tests fail
+        const float m2 = cmax * cmax;                        //  the filter and fall back to FP64)
+        thrArea = filtered ? ldexpf(m2, -17) + 0x1p-50f : INFINITY;
+        thrOrient = filtered ? ldexpf(m2, -17) + 0x1p-60f : INFINITY;
         n.i = i;
         n.prev = n.next = -1;
         n.z = 0;
@@ -102,12 +118,30 @@ struct DevEarcut {
         out[outCnt++] = N[c].i;
     }
 
+    // The reference's area() (:694-699) as far as its callers use it: they compare it with zero only, so a
+    // certified FP32 value stands in for the FP64 one (same sign, not snapped).
     SB_HD double area(int p, int q, int r) const
     {
+        const float vf = (N[q].yf - N[p].yf) * (N[r].xf - N[q].xf) - (N[q].xf - N[p].xf) * (N[r].yf - N[q].yf);
+        if (fabsf(vf) > thrArea)
+            return (double)vf;
         double v = (N[q].y - N[p].y) * (N[r].x - N[q].x) - (N[q].x - N[p].x) * (N[r].y - N[q].y);
         if (fabs(v) <= kDblEps)
             v = 0.0;
         return v;
+    }
+    // one of pointInTriangle's three tests, (c - p) x (a - p) >= 0 in the reference's FP64 form, filtered
+    SB_HD bool orientNonNeg(int a, int c, int p) const
+    {
+        const float ef = (N[c].xf - N[p].xf) * (N[a].yf - N[p].yf) - (N[a].xf - N[p].xf) * (N[c].yf - N[p].yf);
+        if (fabsf(ef) > thrOrient)
+            return ef > 0.f;
+        return (N[c].x - N[p].x) * (N[a].y - N[p].y) - (N[a].x - N[p].x) * (N[c].y - N[p].y) >= 0;
+    }
+    // pointInTriangle on nodes (the ear tests)
+    SB_HD bool nodeInTriangle(int a, int b, int c, int p) const
+    {
+        return orientNonNeg(a, c, p) && orientNonNeg(b, a, p) && orientNonNeg(c, b, p);
     }
     SB_HD bool equals(int a, int b) const { return N[a].x == N[b].x && N[a].y == N[b].y; }
     static SB_HD int sgn(double v) { return (0.0 < v) - (v < 0.0); }
@@ -307,7 +341,7 @@ struct DevEarcut {
             return false;
         int p = N[N[ear].next].next;
         while (p != N[ear].prev && tick()) {
-            if (pointInTriangle(N[a].x, N[a].y, N[b].x, N[b].y, N[c].x, N[c].y, N[p].x, N[p].y) &&
+            if (nodeInTriangle(a, b, c, p) &&
                 area(N[p].prev, p, N[p].next) >= 0)
                 return false;
             p = N[p].next;
@@ -328,7 +362,7 @@ struct DevEarcut {
         int p = N[ear].nextZ;
         while (p >= 0 && N[p].z <= maxZ && tick()) {
             if (p != N[ear].prev && p != N[ear].next &&
-                pointInTriangle(N[a].x, N[a].y, N[b].x, N[b].y, N[c].x, N[c].y, N[p].x, N[p].y) &&
+                nodeInTriangle(a, b, c, p) &&
                 area(N[p].prev, p, N[p].next) >= 0)
                 return false;
             p = N[p].nextZ;
@@ -336,7 +370,7 @@ struct DevEarcut {
         p = N[ear].prevZ;
         while (p >= 0 && N[p].z >= minZ && tick()) {
             if (p != N[ear].prev && p != N[ear].next &&
-                pointInTriangle(N[a].x, N[a].y, N[b].x, N[b].y, N[c].x, N[c].y, N[p].x, N[p].y) &&
+                nodeInTriangle(a, b, c, p) &&
                 area(N[p].prev, p, N[p].next) >= 0)
                 return false;
             p = N[p].prevZ;

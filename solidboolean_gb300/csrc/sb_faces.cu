@@ -585,6 +585,7 @@ SB_HDF FaceOut process_face(const FaceJob &job, const FaceArgs &a, int f, char *
 
     // ---- 5. ear clipping -------------------------------------------------------------------------------
     DevEarcut ec;
+    ec.filtered = a.filteredEarcut != 0;
     ec.N = s.ecNodes;
     ec.cap = D.nodeCap;
     ec.out = s.ecOut;

@@ -29,6 +29,7 @@ struct FaceArgs {
     int robustEdges = 0;  // SB_ROBUST_EDGE_TOLERANCE: scale-relative point-on-edge test (0: the reference's)
     unsigned long long scratchCap = ~0ull; // bytes of scratch; a face whose slice ends past it reports capacity
     const double *frames = nullptr;        // optional: per face its projection axis and perpendicular (6 doubles)
+    int filteredEarcut = 1;                // ear-clipping orientations FP32-filtered (0: plain FP64)
 };
 
 size_t face_scratch_bytes_host(int np);
