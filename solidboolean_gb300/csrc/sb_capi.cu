@@ -1805,7 +1805,19 @@ sb_status sb_mesh_prepare(sb_mesh *m, const sb_options *opts)
         if (opts)
             o = *opts;
         // issued without waiting: sb_combine orders itself after the build and reports its status
-        return prepare_mesh(m, o.order, (cudaStream_t)o.stream, false);
+        cudaStream_t s = (cudaStream_t)o.stream;
+        if (!s) {
+            // no stream given: the build runs on the mesh's own stream, after everything queued so far on the
+            // legacy default stream, so that two meshes prepared one after the other build concurrently
+            if (!m->own) {
+                SB_CUDA_CHECK(cudaStreamCreateWithFlags(&m->own, cudaStreamNonBlocking));
+                SB_CUDA_CHECK(cudaEventCreateWithFlags(&m->ownFork, cudaEventDisableTiming));
+            }
+            SB_CUDA_CHECK(cudaEventRecord(m->ownFork, nullptr));
+            SB_CUDA_CHECK(cudaStreamWaitEvent(m->own, m->ownFork, 0));
+            s = m->own;
+        }
+        return prepare_mesh(m, o.order, s, false);
     });
 }
 
@@ -1821,6 +1833,11 @@ void sb_mesh_destroy(sb_mesh *m)
     pinned_slot_release(m->rankCheck);
     if (m->aux)
         cudaStreamDestroy(m->aux);
+    if (m->own) {
+        cudaStreamSynchronize(m->own);
+        cudaStreamDestroy(m->own);
+        cudaEventDestroy(m->ownFork);
+    }
     if (m->auxFork)
         cudaEventDestroy(m->auxFork);
     if (m->auxJoin)

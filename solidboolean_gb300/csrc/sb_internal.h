@@ -81,6 +81,10 @@ struct sb_mesh {
     bool rankPending = false;      // rankCheck not yet read (build_reference_rank without waiting)
     bool ownsInput = true;
     cudaStream_t stream = nullptr;
+    // preparation stream for callers that pass no stream: a preparation on the legacy default stream would
+    // serialise the builds of two meshes; this one forks from it instead (created on first use)
+    cudaStream_t own = nullptr;
+    cudaEvent_t ownFork = nullptr;
     std::vector<double> hostV;    // only for host-created meshes (kept for re-preparation)
     std::vector<uint32_t> hostT;
 };
