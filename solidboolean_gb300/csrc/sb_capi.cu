@@ -668,6 +668,7 @@ struct sb_boolean {
     cudaStream_t side = nullptr;     // second stream for preparing the two meshes concurrently
     cudaEvent_t sideDone = nullptr;
     cudaEvent_t orderDone = nullptr; // the cut faces' processing order, computed on `side`
+    cudaEvent_t retriDone = nullptr; // the re-triangulated triangles' numbering, computed on `side`
     bool evInit = false;
     char *mail = nullptr; // pinned mailbox: small reads [0, kMailRead), constant uploads after it
 };
@@ -784,6 +785,8 @@ sb_status combine_impl(sb_boolean *b)
     }
     if (!b->orderDone)
         SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->orderDone, cudaEventDisableTiming));
+    if (!b->retriDone)
+        SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->retriDone, cudaEventDisableTiming));
     // the meshes may have been prepared on other streams
     for (const sb_mesh *cm : {b->first, b->second})
         if (cm->readyEv)
@@ -1137,6 +1140,32 @@ sb_status combine_impl(sb_boolean *b)
     SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
         return cub::DeviceScan::ExclusiveSum(tmp, bytes, notB, g.uncutRankB, nB + 1, s);
     }));
+    // the global weld's tables, filled while the leaf orders finish
+    const size_t nSeq = (size_t)totals[1];
+    const uint32_t weldCap = pow2_at_least(2 * nSeq + 2);
+    Carve cw;
+    size_t o_wo = cw.take<int>(weldCap), o_wm = cw.take<int>(weldCap), o_ps = cw.take<int>(nSeq + 1);
+    size_t o_if = cw.take<int>(nSeq + 1), o_fr = cw.take<int>(nSeq + 1), o_sr = cw.take<int>(weldCap);
+    size_t o_nsrc = cw.take<int>(nSeq + 1);
+    SB_CUDA_CHECK(b->weld.ensure(cw.off));
+    char *wb = b->weld.as<char>();
+    g.weldOwner = (int *)(wb + o_wo);
+    g.weldMin = (int *)(wb + o_wm);
+    g.weldMask = weldCap - 1;
+    g.pointSlot = (int *)(wb + o_ps);
+    g.isFirst = (int *)(wb + o_if);
+    g.firstRank = (int *)(wb + o_fr);
+    g.slotRank = (int *)(wb + o_sr);
+    g.newSrc = (int *)(wb + o_nsrc);
+    b->d_newSrc = g.newSrc;
+    b->newBase = A.nv + B.nv;
+    {
+        Fills fl(s);
+        fl.i32(g.weldOwner, weldCap, -1);
+        fl.i32(g.weldMin, weldCap, INT_MAX);
+        fl.i32(g.isFirst, nSeq + 1, 0);
+        fl.launch();
+    }
     // from here on the leaf orders are needed
     {
         const sb_status r = waitRanks();
@@ -1204,6 +1233,23 @@ sb_status combine_impl(sb_boolean *b)
         fa.filteredEarcut = fp64 ? 0 : 1;
         launch_faces(fa, s);
         SB_CUDA_CHECK(cudaGetLastError());
+        // the re-triangulated triangles are numbered in the faces' processing order: on the second stream,
+        // after the processing order and the re-triangulation, beside the weld
+        SB_CUDA_CHECK(cudaEventRecord(b->sideDone, s)); // re-recorded: earlier waits hold their own records
+        SB_CUDA_CHECK(cudaStreamWaitEvent(b->side, b->sideDone, 0));
+        RankScanArgs rr;
+        std::memset(&rr, 0, sizeof rr);
+        rr.n = nFaces;
+        rr.FA = FA;
+        rr.count = 1;
+        rr.faceByRank = faceByRank;
+        rr.faceRank = faceRank;
+        rr.vals[0] = faceNtris;
+        rr.out[0] = retriRank;
+        rr.tmp[0] = rankTmp[2];
+        rr.tot[0] = rankTot + 4;
+        launch_rank_scan(rr, b->side);
+        SB_CUDA_CHECK(cudaEventRecord(b->retriDone, b->side));
     }
     SB_CUDA_CHECK(cudaEventRecord(b->ev[3], s));
 
@@ -1235,32 +1281,7 @@ sb_status combine_impl(sb_boolean *b)
     g.faceEdges = faceEdges;
     g.counters = d_counters;
     g.newBase = A.nv + B.nv;
-    const size_t nSeq = (size_t)totals[1];
-    const uint32_t weldCap = pow2_at_least(2 * nSeq + 2);
-    Carve cw;
-    size_t o_wo = cw.take<int>(weldCap), o_wm = cw.take<int>(weldCap), o_ps = cw.take<int>(nSeq + 1);
-    size_t o_if = cw.take<int>(nSeq + 1), o_fr = cw.take<int>(nSeq + 1), o_sr = cw.take<int>(weldCap);
-    size_t o_nsrc = cw.take<int>(nSeq + 1);
-    SB_CUDA_CHECK(b->weld.ensure(cw.off));
-    char *wb = b->weld.as<char>();
-    g.weldOwner = (int *)(wb + o_wo);
-    g.weldMin = (int *)(wb + o_wm);
-    g.weldMask = weldCap - 1;
-    g.pointSlot = (int *)(wb + o_ps);
-    g.isFirst = (int *)(wb + o_if);
-    g.firstRank = (int *)(wb + o_fr);
-    g.slotRank = (int *)(wb + o_sr);
     g.ptSrc = ptSrc;
-    g.newSrc = (int *)(wb + o_nsrc);
-    b->d_newSrc = g.newSrc;
-    b->newBase = A.nv + B.nv;
-    {
-        Fills fl(s);
-        fl.i32(g.weldOwner, weldCap, -1);
-        fl.i32(g.weldMin, weldCap, INT_MAX);
-        fl.i32(g.isFirst, nSeq + 1, 0);
-        fl.launch();
-    }
     if (orderPending)
         SB_CUDA_CHECK(cudaStreamWaitEvent(s, b->orderDone, 0));
     launch_weld(g, s);
@@ -1270,21 +1291,8 @@ sb_status combine_impl(sb_boolean *b)
     // the number of welded points is read with the arrangement's counts below (nothing before needs it)
     int nNew = 0;
 
-    if (nFaces > 0) {
-        // the re-triangulated triangles are numbered in the faces' processing order
-        RankScanArgs ra;
-        std::memset(&ra, 0, sizeof ra);
-        ra.n = nFaces;
-        ra.FA = FA;
-        ra.count = 1;
-        ra.faceByRank = faceByRank;
-        ra.faceRank = faceRank;
-        ra.vals[0] = faceNtris;
-        ra.out[0] = retriRank;
-        ra.tmp[0] = rankTmp[2];
-        ra.tot[0] = rankTot + 4;
-        launch_rank_scan(ra, s);
-    }
+    if (nFaces > 0)
+        SB_CUDA_CHECK(cudaStreamWaitEvent(s, b->retriDone, 0));
     (void)retriRef;
     int cnts[4] = {0, 0, 0, 0}; // uncutA, uncutB, retriA, retri total
     {
@@ -2105,6 +2113,8 @@ void sb_boolean_destroy(sb_boolean *b)
             cudaEventDestroy(e);
     if (b->orderDone)
         cudaEventDestroy(b->orderDone);
+    if (b->retriDone)
+        cudaEventDestroy(b->retriDone);
     if (b->side) {
         cudaStreamDestroy(b->side);
         cudaEventDestroy(b->sideDone);
