@@ -198,6 +198,19 @@ def batch(n_pairs: int = 4096, seed: int = 1234, max_level: int = 5):
     return [batch_pair(rng, max_level) for _ in range(n_pairs)]
 
 
+def interpenetrating(seed: int = 7, level: int = 5, rel: float = 0.005):
+    """Two unit icospheres of one level, the second randomly rotated, both jittered radially by U(-rel, +rel):
+    the surfaces cross each other all over, so a large share of both meshes' triangles is cut (about 15.7 k
+    cut faces per mesh at level 5, 63 k at level 6) into many small loops."""
+    rng = SplitMix64(seed)
+    va, fa = icosphere(level)
+    vb, fb = icosphere(level)
+    va = jitter_radial(va, rng, rel)
+    vb = transform(vb, 1.0, rotation_matrix(rng.unit_quaternion()))
+    vb = jitter_radial(np.ascontiguousarray(vb), rng, rel)
+    return np.ascontiguousarray(va), fa, np.ascontiguousarray(vb), fb
+
+
 def diff_volume(seed: int = 1234, level: int = 5, sigma: float = 0.01):
     rng = SplitMix64(seed)
     va, fa = icosphere(level)

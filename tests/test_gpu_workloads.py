@@ -72,3 +72,16 @@ def test_headline_reference_digests(gpu_lib, name):
     assert input_digest(va, fa, vb, fb) == want["inputs"]
     got = sbg.run_boolean(va, fa, vb, fb, want["quantum"])
     assert digests(got, len(va) + len(vb), want["quantum"]) == {k: v for k, v in want.items() if k not in META}
+
+
+@pytest.mark.parametrize("level", [5, 6])
+def test_interpenetrating_many_cut_faces(gpu_lib, port, level):
+    """Two jittered unit spheres crossing each other everywhere: 15.7 k (level 5) and 63 k (level 6) cut faces
+    per mesh, tens of thousands of small loops. Past 8,192 faces per mesh the faces are sorted device-wide,
+    past 65,536 faces the face layout is scanned device-wide, and the loop order's work arrays leave shared
+    memory. Strict at weld factor 1e8; at 1e5 the reference fails and so must the library."""
+    va, fa, vb, fb = mg.interpenetrating(7, level)
+    ref, got = _check(port, va, fa, vb, fb, 100000000)
+    assert ref["status"] == 1 and got["stats"]["cut_faces_first"] > 8192
+    ref, got = _check(port, va, fa, vb, fb, 100000)
+    assert ref["status"] == 0 and got["code"] in (sbg.SB_FAIL_ATTACH, sbg.SB_FAIL_LINK, sbg.SB_FAIL_LOOP)
