@@ -689,9 +689,10 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
                     hit = ray.qlo[0] <= bx[3] && ray.qhi[0] >= bx[0] && ray.qlo[1] <= bx[4] && ray.qhi[1] >= bx[1] &&
                           ray.qlo[2] <= bx[5] && ray.qhi[2] >= bx[2];
                 } else {
-                    const float *bx = M.nbox32 + 6 * (size_t)c;
-                    hit = ray.olo[0] <= bx[3] && ray.ohi[0] >= bx[0] && ray.olo[1] <= bx[4] && ray.ohi[1] >= bx[1] &&
-                          ray.olo[2] <= bx[5] && ray.ohi[2] >= bx[2];
+                    const float4 *bx = reinterpret_cast<const float4 *>(M.nbox32) + 2 * (size_t)c;
+                    const float4 lo = __ldg(bx), hi = __ldg(bx + 1);
+                    hit = ray.olo[0] <= hi.x && ray.ohi[0] >= lo.x && ray.olo[1] <= hi.y && ray.ohi[1] >= lo.y &&
+                          ray.olo[2] <= hi.z && ray.ohi[2] >= lo.z;
                 }
                 if (hit)
                     push[k] = c;

@@ -152,7 +152,7 @@ static size_t mesh_layout_bytes(int nv, int nt)
     c.take<int>((size_t)nt);
     c.take<int2>((size_t)(nt > 1 ? nt - 1 : 1));
     c.take<int>((size_t)(2 * nt));
-    c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 8);
     c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
     c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
     c.take<int>((size_t)nt);

@@ -47,7 +47,7 @@ struct MeshDev {
     int *leafTri = nullptr;   // [nt] triangle at each Morton-ordered leaf
     int2 *child = nullptr;    // [nt-1] (left, right)
     int *parent = nullptr;    // [2*nt-1]: internal nodes then leaves (offset nt-1)
-    float *nbox32 = nullptr;  // [(nt-1)*6]
+    float *nbox32 = nullptr;  // [(nt-1)*8]: lo xyz, 0, hi xyz, 0 (two 16-byte loads per node)
     double *nbox64 = nullptr; // [(nt-1)*6]
     int *flags = nullptr;     // [nt-1] refit arrival counters
     int *rank = nullptr;      // [nt] position of each triangle in the reference tree's leaf order

@@ -115,9 +115,10 @@ __global__ void __launch_bounds__(128) k_broad(MeshDev A, MeshDev B, uint64_t *o
                             hit = q64[0] <= bx[3] && q64[3] >= bx[0] && q64[1] <= bx[4] && q64[4] >= bx[1] &&
                                   q64[2] <= bx[5] && q64[5] >= bx[2];
                         } else {
-                            const float *bx = B.nbox32 + 6 * (size_t)c;
-                            hit = qo[0] <= bx[3] && qo[3] >= bx[0] && qo[1] <= bx[4] && qo[4] >= bx[1] &&
-                                  qo[2] <= bx[5] && qo[5] >= bx[2];
+                            const float4 *bx = reinterpret_cast<const float4 *>(B.nbox32) + 2 * (size_t)c;
+                            const float4 lo = __ldg(bx), hi = __ldg(bx + 1);
+                            hit = qo[0] <= hi.x && qo[3] >= lo.x && qo[1] <= hi.y && qo[4] >= lo.y &&
+                                  qo[2] <= hi.z && qo[5] >= lo.z;
                         }
                         if (hit) {
                             if (sp < 96)

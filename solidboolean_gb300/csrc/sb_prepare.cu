@@ -214,9 +214,11 @@ __global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__
         for (int k = 0; k < 3; ++k) {
             nbox64[6 * (size_t)node + k] = m[k];
             nbox64[6 * (size_t)node + 3 + k] = m[3 + k];
-            nbox32[6 * (size_t)node + k] = __double2float_rd(m[k]);
-            nbox32[6 * (size_t)node + 3 + k] = __double2float_ru(m[3 + k]);
         }
+        reinterpret_cast<float4 *>(nbox32)[2 * (size_t)node] =
+            make_float4(__double2float_rd(m[0]), __double2float_rd(m[1]), __double2float_rd(m[2]), 0.f);
+        reinterpret_cast<float4 *>(nbox32)[2 * (size_t)node + 1] =
+            make_float4(__double2float_ru(m[3]), __double2float_ru(m[4]), __double2float_ru(m[5]), 0.f);
         cur = node;
         node = parent[node];
     }
@@ -311,7 +313,7 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
     size_t o_lt = c.take<int>((size_t)nt);
     size_t o_ch = c.take<int2>((size_t)(nt > 1 ? nt - 1 : 1));
     size_t o_pa = c.take<int>((size_t)(2 * nt));
-    size_t o_n32 = c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
+    size_t o_n32 = c.take<float>((size_t)(nt > 1 ? nt - 1 : 1) * 8);
     size_t o_n64 = c.take<double>((size_t)(nt > 1 ? nt - 1 : 1) * 6);
     size_t o_fl = c.take<int>((size_t)(nt > 1 ? nt - 1 : 1));
     size_t o_rk = c.take<int>((size_t)nt);
