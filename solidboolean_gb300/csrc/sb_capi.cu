@@ -994,6 +994,7 @@ sb_status combine_impl(sb_boolean *b)
     bool orderPending = false;
     FaceOrderArgs fo;   // the faces' processing order (second stream), set up with the face capacities
     RankScanArgs ra;
+    int *rankPart2 = nullptr;
     char *ob = nullptr;
     size_t o_fks = 0, o_fvs = 0;
     if (nFaces > 0) {
@@ -1033,7 +1034,7 @@ sb_status combine_impl(sb_boolean *b)
         const size_t o_hA = co.take<int>(hash_scratch_ints(FA)), o_hB = co.take<int>(hash_scratch_ints(FB));
         const size_t o_pr = co.take<int>(nFaces + 1), o_er = co.take<int>(nFaces + 1), o_rr2 = co.take<int>(nFaces + 1);
         const size_t o_t0 = co.take<int>(nFaces + 1), o_t1 = co.take<int>(nFaces + 1), o_t2 = co.take<int>(nFaces + 1);
-        const size_t o_tot = co.take<int>(8);
+        const size_t o_tot = co.take<int>(8), o_part = co.take<int>(3 * 1024), o_part2 = co.take<int>(3 * 1024);
         SB_CUDA_CHECK(b->order.ensure(co.off));
         ob = b->order.as<char>();
         fo.nFaces = nFaces;
@@ -1080,6 +1081,8 @@ sb_status combine_impl(sb_boolean *b)
         ra.tmp[1] = rankTmp[1];
         ra.tot[0] = rankTot;
         ra.tot[1] = rankTot + 2;
+        ra.part = (int *)(ob + o_part);
+        rankPart2 = (int *)(ob + o_part2); // its own: the triangles' numbering may overlap this scan
         // The totals follow from the pair count without a read-back: every intersecting pair cuts one face of
         // each mesh, so the faces' pair counts sum to 2 K; a face of np pairs takes 2 np points, 2 np directed
         // edges and 32 np + 16 triangles. Its scratch is bounded by an affine function of np
@@ -1248,6 +1251,7 @@ sb_status combine_impl(sb_boolean *b)
         rr.out[0] = retriRank;
         rr.tmp[0] = rankTmp[2];
         rr.tot[0] = rankTot + 4;
+        rr.part = rankPart2;
         launch_rank_scan(rr, b->side);
         SB_CUDA_CHECK(cudaEventRecord(b->retriDone, b->side));
     }

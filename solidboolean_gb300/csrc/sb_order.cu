@@ -410,12 +410,103 @@ __global__ void __launch_bounds__(kOrderThreads) k_rank_scan(RankScanArgs a)
     }
 }
 
+// The multi-block form for many faces: values gathered in rank order with per-block sums (blockIdx.y = the
+// array), the block sums scanned by one block, then each block scans its chunk from its offset, and the
+// results are scattered back to face order.
+constexpr int kRankScanBlockMax = 16384; // faces up to which one block per array scans
+constexpr int kRankChunk = 1024;         // ranks per block in the multi-block form
+
+__global__ void __launch_bounds__(kRankChunk) k_rank_gather(RankScanArgs a, int nb)
+{
+    const int k = blockIdx.y, r = blockIdx.x * kRankChunk + threadIdx.x;
+    const int v = r < a.n ? a.vals[k][a.faceByRank[r]] : 0;
+    if (r < a.n)
+        a.tmp[k][r] = v;
+    int s = v;
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    __shared__ int ws[32];
+    if ((threadIdx.x & 31) == 0)
+        ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kRankChunk / 32; ++w)
+            t += ws[w];
+        a.part[k * nb + blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_rank_parts(RankScanArgs a, int nb)
+{
+    for (int k = 0; k < a.count; ++k) {
+        const int total = block_excl_scan(a.part + k * nb, nb);
+        if (threadIdx.x == 0)
+            a.tot[k][1] = total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kRankChunk) k_rank_chunk_scan(RankScanArgs a, int nb)
+{
+    const int k = blockIdx.y, r = blockIdx.x * kRankChunk + threadIdx.x, lane = threadIdx.x & 31,
+              w = threadIdx.x >> 5;
+    const int v = r < a.n ? a.tmp[k][r] : 0;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o)
+            incl += t;
+    }
+    __shared__ int ws[32];
+    if (lane == 31)
+        ws[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const int x = ws[lane];
+        int y = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xFFFFFFFFu, y, o);
+            if (lane >= o)
+                y += t;
+        }
+        ws[lane] = y - x;
+    }
+    __syncthreads();
+    const int excl = a.part[k * nb + blockIdx.x] + ws[w] + incl - v;
+    if (r < a.n)
+        a.tmp[k][r] = excl;
+    if (r == a.FA && a.FA < a.n)
+        a.tot[k][0] = excl;
+}
+
+__global__ void k_rank_scatter(RankScanArgs a)
+{
+    const int k = blockIdx.y, f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < a.n)
+        a.out[k][f] = a.tmp[k][a.faceRank[f]];
+    if (f == 0) {
+        a.out[k][a.n] = a.tot[k][1];
+        if (a.FA >= a.n)
+            a.tot[k][0] = a.tot[k][1];
+    }
+}
+
 void launch_rank_scan(const RankScanArgs &a, cudaStream_t s)
 {
     if (a.n <= 0 || a.count <= 0)
         return;
     KTime kt("k_rank_scan", s);
-    SB_COUNT(k_rank_scan)<<<a.count, kOrderThreads, 0, s>>>(a);
+    const int nb = (a.n + kRankChunk - 1) / kRankChunk;
+    if (a.n <= kRankScanBlockMax || !a.part || nb > 1024) {
+        SB_COUNT(k_rank_scan)<<<a.count, kOrderThreads, 0, s>>>(a);
+        return;
+    }
+    const dim3 g(nb, a.count);
+    SB_COUNT(k_rank_gather)<<<g, kRankChunk, 0, s>>>(a, nb);
+    SB_COUNT(k_rank_parts)<<<1, kOrderThreads, 0, s>>>(a, nb);
+    SB_COUNT(k_rank_chunk_scan)<<<g, kRankChunk, 0, s>>>(a, nb);
+    SB_COUNT(k_rank_scatter)<<<dim3((a.n + 255) / 256, a.count), 256, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------------------------------

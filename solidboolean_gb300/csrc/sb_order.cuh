@@ -59,6 +59,7 @@ struct RankScanArgs {
     int *out[3];   // [n + 1]
     int *tmp[3];   // [n + 1] scratch
     int *tot[3];   // [2]
+    int *part;     // [3 * 1024] block partial sums (the multi-block form, past kRankScanBlockMax faces)
 };
 void launch_rank_scan(const RankScanArgs &a, cudaStream_t s);
 
