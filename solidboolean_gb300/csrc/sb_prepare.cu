@@ -202,9 +202,13 @@ __global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__
     int cur = ~i; // child id of leaf i
     int node = parent[(n - 1) + i];
     while (node >= 0) {
+        // the hierarchy does not change during the refit: the node's children and parent are loaded before
+        // the arrival, so that their latency overlaps the atomic's (two dependent round trips per level, the
+        // arrival and the sibling's box, instead of four)
+        const int2 ch = child[node];
+        const int up = parent[node];
         if (arrive_acq_rel(flags + node) == 0)
             return;
-        const int2 ch = child[node];
         const int sib = ch.x == cur ? ch.y : ch.x;
         const double *sb = sib < 0 ? box64 + 6 * (size_t)__ldcg(leafTri + ~sib) : nbox64 + 6 * (size_t)sib;
         for (int k = 0; k < 3; ++k) {
@@ -220,7 +224,7 @@ __global__ void k_refit(int n, const int *__restrict__ leafTri, const double *__
         reinterpret_cast<float4 *>(nbox32)[2 * (size_t)node + 1] =
             make_float4(__double2float_ru(m[3]), __double2float_ru(m[4]), __double2float_ru(m[5]), 0.f);
         cur = node;
-        node = parent[node];
+        node = up;
     }
 }
 
