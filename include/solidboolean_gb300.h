@@ -116,6 +116,9 @@ uint64_t sb_kernel_launches(void);
 void sb_kernel_timing(int enable);
 int sb_kernel_timing_read(const char *name, double *total_ms, uint64_t *launches);
 int sb_kernel_timing_names(char *buf, size_t cap);
+/* Restrict the timing to the named kernels (comma-separated; NULL or "" for all). Each timed launch adds an
+ * event pair to its stream, so a timed run is slower the more kernels it times. */
+void sb_kernel_timing_select(const char *names);
 
 /* Mesh: vertices are FP64 xyz triplets, triangles are uint32 index triplets. The host variant copies
  * the arrays; the device variant copies from device pointers on opts->stream. */

@@ -44,12 +44,15 @@ static std::mutex g_kt_mutex;
 static std::vector<KRec> g_kt_recs;
 static size_t g_kt_used = 0;
 static std::atomic<bool> g_kt_on{false};
+static std::string g_kt_only; // ",name,name," or empty for every kernel
 
 bool ktime_enabled() { return g_kt_on.load(std::memory_order_relaxed); }
 
 int ktime_begin(const char *name, cudaStream_t s)
 {
     std::lock_guard<std::mutex> lk(g_kt_mutex);
+    if (!g_kt_only.empty() && g_kt_only.find("," + std::string(name) + ",") == std::string::npos)
+        return -1;
     if (g_kt_used == g_kt_recs.size()) {
         KRec r;
         if (cudaEventCreate(&r.a) != cudaSuccess || cudaEventCreate(&r.b) != cudaSuccess)
@@ -1659,6 +1662,12 @@ void sb_kernel_timing(int enable)
     std::lock_guard<std::mutex> lk(g_kt_mutex);
     g_kt_used = 0;
     g_kt_on.store(enable != 0);
+}
+
+void sb_kernel_timing_select(const char *names)
+{
+    std::lock_guard<std::mutex> lk(g_kt_mutex);
+    g_kt_only = names && *names ? "," + std::string(names) + "," : std::string();
 }
 
 int sb_kernel_timing_read(const char *name, double *total_ms, uint64_t *launches)

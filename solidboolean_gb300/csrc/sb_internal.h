@@ -51,6 +51,7 @@ struct MeshDev {
     double *nbox64 = nullptr; // [(nt-1)*6]
     int *flags = nullptr;     // [nt-1] refit arrival counters
     int *rank = nullptr;      // [nt] position of each triangle in the reference tree's leaf order
+    const unsigned int *absMax = nullptr; // [3] per axis: largest |box coordinate|, rounded up to FP32 (bits)
     // the reference tree's nodes: {first leaf position, member count, left child id (the right child is
     // left + 1), -1 for a leaf}; node 0 is the root. Valid with rank.
     int4 *tnode = nullptr;

@@ -16,12 +16,13 @@
 
 namespace sbg {
 
-// FP32 vertex copies; thread 0 also resets the 8 words of centre bounds that k_tri_boxes accumulates
-// (min keys at all ones, max keys and the rest at zero)
+// FP32 vertex copies; threads 0-11 also reset the 12 words that k_tri_boxes accumulates: the centre bounds
+// (min keys at all ones, max keys at zero), two unused words, and the per-axis largest |coordinate| (zero)
+constexpr int kBoundWords = 12;
 __global__ void k_vertices_f32(int nv, const double *__restrict__ v, float4 *__restrict__ vf, unsigned int *bounds)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 8)
+    if (i < kBoundWords)
         bounds[i] = i < 3 ? 0xFFFFFFFFu : 0u;
     if (i >= nv)
         return;
@@ -37,6 +38,7 @@ __global__ void k_tri_boxes(int nt, const double *__restrict__ v, const uint32_t
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float c[3] = {0.f, 0.f, 0.f};
+    unsigned int amax[3] = {0u, 0u, 0u}; // FP32 bits of the largest |coordinate|, rounded up
     bool valid = i < nt;
     if (valid) {
         double lo[3] = {kDblMax, kDblMax, kDblMax};
@@ -59,34 +61,40 @@ __global__ void k_tri_boxes(int nt, const double *__restrict__ v, const uint32_t
             box32[6 * (size_t)i + 3 + a] = h;
             c[a] = 0.5f * l + 0.5f * h;
             cen[3 * (size_t)i + a] = c[a];
+            amax[a] = __float_as_uint(__double2float_ru(fmax(fabs(lo[a]), fabs(hi[a]))));
         }
     }
     // block-wide min/max of the centres, then one atomic per block and axis (ordered-int encoding)
-    __shared__ unsigned int smin[3][32], smax[3][32];
+    __shared__ unsigned int smin[3][32], smax[3][32], sabs[3][32];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int a = 0; a < 3; ++a) {
         unsigned int u = __float_as_uint(c[a]);
         unsigned int o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
         unsigned int mn = valid ? o : 0xFFFFFFFFu, mx = valid ? o : 0u;
+        unsigned int am = amax[a]; // non-negative floats order as their bits
         for (int s = 16; s > 0; s >>= 1) {
             mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, s));
             mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, s));
+            am = max(am, __shfl_xor_sync(0xFFFFFFFFu, am, s));
         }
         if (lane == 0) {
             smin[a][warp] = mn;
             smax[a][warp] = mx;
+            sabs[a][warp] = am;
         }
     }
     __syncthreads();
     if (threadIdx.x < 3) {
         int a = threadIdx.x;
-        unsigned int mn = 0xFFFFFFFFu, mx = 0u;
+        unsigned int mn = 0xFFFFFFFFu, mx = 0u, am = 0u;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
             mn = min(mn, smin[a][w]);
             mx = max(mx, smax[a][w]);
+            am = max(am, sabs[a][w]);
         }
         atomicMin(bounds + a, mn);
         atomicMax(bounds + 3 + a, mx);
+        atomicMax(bounds + 8 + a, am);
     }
 }
 
@@ -358,7 +366,7 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
                                     (int *)nullptr, nt, 0, 30, s);
     Carve tc;
     size_t t_cen = tc.take<float>((size_t)nt * 3);
-    size_t t_bnd = tc.take<unsigned int>(8);
+    size_t t_bnd = tc.take<unsigned int>(kBoundWords);
     size_t t_key = tc.take<uint32_t>((size_t)nt);
     size_t t_idx = tc.take<int>((size_t)nt);
     size_t t_cub = tc.take<char>(sortBytes);
@@ -370,6 +378,7 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
     float *cen = reinterpret_cast<float *>(tb + t_cen);
     unsigned int *bounds = reinterpret_cast<unsigned int *>(tb + t_bnd);
     uint32_t *keyIn = reinterpret_cast<uint32_t *>(tb + t_key);
+    d.absMax = bounds + 8; // the leaf order's fixed-point grids
     int *idxIn = reinterpret_cast<int *>(tb + t_idx);
 
     const int BS = 256;

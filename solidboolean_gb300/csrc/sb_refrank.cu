@@ -466,101 +466,20 @@ __global__ void k_rr_init(RNode *nodes, NParam *np, int nt, int *counters, unsig
     counters[kCtNodes] = 1;
 }
 
-// Box centre of each triangle as AxisAlignedBoudingBox::updateCenter computes it, (((0 + v0) + v1) + v2) /
-// (float)3 (src/axisalignedboundingbox.h:31-53), its box, and the root box (src/solidmesh.cpp:68-72).
-// Records are stored in Morton order (position p holds triangle leafTri[p]): member order is carried by the
-// direction bits, so the processing order is free, and in Morton order a node's members form long runs.
-__global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double *__restrict__ v,
-                                                           const uint32_t *__restrict__ t,
-                                                           const double *__restrict__ box64,
-                                                           const int *__restrict__ leafTri, RRec *rec,
-                                                           unsigned long long *soa, int *posOf, int *state,
-                                                           RNode *nodes)
+// Split parameters of the root (or the root listed as a terminal node when it is small), from its box and
+// fixed-point sum.
+__device__ void root_params(RNode *nodes, NParam *np, int nt, const int *sc, int *counters, int *terms)
 {
-    __shared__ unsigned long long sLo[3], sHi[3];
-    if (threadIdx.x < 3) {
-        sLo[threadIdx.x] = ~0ull;
-        sHi[threadIdx.x] = 0ull;
-    }
-    __syncthreads();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
-    if (p < nt) {
-        const int i = leafTri[p];
-        RRec r;
-        for (int a = 0; a < 3; ++a) {
-            double s = 0.0;
-            for (int k = 0; k < 3; ++k)
-                s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
-            r.c[a] = ordc(div3_rn(s));
-            lo[a] = r.lo[a] = ordc(box64[6 * (size_t)i + a]);
-            hi[a] = r.hi[a] = ordc(box64[6 * (size_t)i + 3 + a]);
-            r.fx[a] = 0; // filled once the grid exponents are known (k_rr_root_sum)
-            soa[(size_t)a * nt + p] = r.c[a];
-            soa[(size_t)(3 + a) * nt + p] = r.lo[a];
-            soa[(size_t)(6 + a) * nt + p] = r.hi[a];
-        }
-        rec[p] = r;
-        posOf[i] = p;
-        state[p] = 0;
-    }
-    for (int o = 16; o > 0; o >>= 1)
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = min(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], o));
-            hi[a] = max(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], o));
-        }
-    if ((threadIdx.x & 31) == 0)
-        for (int a = 0; a < 3; ++a) {
-            atomicMin(&sLo[a], lo[a]);
-            atomicMax(&sHi[a], hi[a]);
-        }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        atomicMin(&nodes[0].st.lo[threadIdx.x], sLo[threadIdx.x]);
-        atomicMax(&nodes[0].st.hi[threadIdx.x], sHi[threadIdx.x]);
-    }
-}
-
-__global__ void __launch_bounds__(kElemThreads) k_rr_root_sum(int nt, RRec *rec, unsigned long long *soa,
-                                                              RNode *nodes, int *scg)
-{
-    __shared__ long long sSum[3];
-    __shared__ int sc[3];
-    if (threadIdx.x < 3) {
-        const int a = threadIdx.x;
-        double M = fmax(fabs(ord_to_dbl(nodes[0].st.lo[a])), fabs(ord_to_dbl(nodes[0].st.hi[a])));
-        sc[a] = fixed_scale(M, nt);
-        sSum[a] = 0;
-        if (blockIdx.x == 0)
-            scg[a] = sc[a];
-    }
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    long long s[3] = {0, 0, 0};
-    if (i < nt)
-        for (int a = 0; a < 3; ++a) {
-            s[a] = to_fixed(ord_to_dbl(rec[i].c[a]), sc[a]);
-            rec[i].fx[a] = s[a];
-            soa[(size_t)(9 + a) * nt + i] = (unsigned long long)s[a];
-        }
-    for (int o = 16; o > 0; o >>= 1)
-        for (int a = 0; a < 3; ++a)
-            s[a] += __shfl_xor_sync(0xFFFFFFFFu, s[a], o);
-    if ((threadIdx.x & 31) == 0)
-        for (int a = 0; a < 3; ++a)
-            atomicAdd(reinterpret_cast<unsigned long long *>(&sSum[a]), (unsigned long long)s[a]);
-    __syncthreads();
-    if (threadIdx.x < 3)
-        atomicAdd(reinterpret_cast<unsigned long long *>(&nodes[0].st.sum[threadIdx.x]),
-                  (unsigned long long)sSum[threadIdx.x]);
-}
-
-__global__ void k_rr_root_params(RNode *nodes, NParam *np, int nt, const int *scg, int *counters, int *terms)
-{
-    RNode &r = nodes[0];
     if (nt > kSub) {
+        unsigned long long lo[3], hi[3];
+        long long sum[3];
+        for (int k = 0; k < 3; ++k) { // other blocks' atomics: read through L2
+            lo[k] = __ldcg(&nodes[0].st.lo[k]);
+            hi[k] = __ldcg(&nodes[0].st.hi[k]);
+            sum[k] = __ldcg(&nodes[0].st.sum[k]);
+        }
         NParam q{-1, nt, 0, 0, 0ull, 0ull};
-        node_params(r.st.lo, r.st.hi, r.st.sum, nt, scg, q.axis, q.clo, q.chi);
+        node_params(lo, hi, sum, nt, sc, q.axis, q.clo, q.chi);
         np[0] = q;
         counters[kCtFirst] = 0;
         counters[kCtLast] = 1;
@@ -572,6 +491,95 @@ __global__ void k_rr_root_params(RNode *nodes, NParam *np, int nt, const int *sc
     }
 }
 
+// Box centre of each triangle as AxisAlignedBoudingBox::updateCenter computes it, (((0 + v0) + v1) + v2) /
+// (float)3 (src/axisalignedboundingbox.h:31-53), its box, its fixed-point centre, and the root's box and
+// fixed-point sum (src/solidmesh.cpp:68-72); the last block to finish computes the root's split parameters.
+// Records are stored in Morton order (position p holds triangle leafTri[p]): member order is carried by the
+// direction bits, so the processing order is free, and in Morton order a node's members form long runs.
+// The fixed-point grid of each axis comes from an upper bound of the coordinates' magnitude (absMax: the
+// triangle boxes' largest |coordinate|, rounded up to FP32, from the preparation's box pass) rather than
+// from the root box, so that no second pass over the members waits for the root box. Any grid that keeps
+// the sums in range gives the same leaf order: the fixed-point sums only bound the reference's mean, and
+// members inside the bound are resolved exactly.
+__global__ void __launch_bounds__(kElemThreads) k_rr_elems(int nt, const double *__restrict__ v,
+                                                           const uint32_t *__restrict__ t,
+                                                           const double *__restrict__ box64,
+                                                           const int *__restrict__ leafTri, RRec *rec,
+                                                           unsigned long long *soa, int *posOf, int *state,
+                                                           RNode *nodes, NParam *np, int *counters, int *terms,
+                                                           int *scg, const unsigned int *__restrict__ absMax,
+                                                           unsigned int *ticket)
+{
+    __shared__ unsigned long long sLo[3], sHi[3];
+    __shared__ long long sSum[3];
+    __shared__ int sc[3];
+    __shared__ bool lastBlock;
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        sLo[a] = ~0ull;
+        sHi[a] = 0ull;
+        sSum[a] = 0;
+        sc[a] = fixed_scale((double)__uint_as_float(absMax[a]), nt);
+        if (blockIdx.x == 0)
+            scg[a] = sc[a];
+    }
+    __syncthreads();
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    long long fs[3] = {0, 0, 0};
+    if (p < nt) {
+        const int i = leafTri[p];
+        RRec r;
+        for (int a = 0; a < 3; ++a) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k)
+                s = s + v[3 * (size_t)t[3 * (size_t)i + k] + a];
+            const double c = div3_rn(s);
+            r.c[a] = ordc(c);
+            lo[a] = r.lo[a] = ordc(box64[6 * (size_t)i + a]);
+            hi[a] = r.hi[a] = ordc(box64[6 * (size_t)i + 3 + a]);
+            fs[a] = r.fx[a] = to_fixed(c, sc[a]);
+            soa[(size_t)a * nt + p] = r.c[a];
+            soa[(size_t)(3 + a) * nt + p] = r.lo[a];
+            soa[(size_t)(6 + a) * nt + p] = r.hi[a];
+            soa[(size_t)(9 + a) * nt + p] = (unsigned long long)r.fx[a];
+        }
+        rec[p] = r;
+        posOf[i] = p;
+        state[p] = 0;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = min(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], o));
+            hi[a] = max(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], o));
+            fs[a] += __shfl_xor_sync(0xFFFFFFFFu, fs[a], o);
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&sLo[a], lo[a]);
+            atomicMax(&sHi[a], hi[a]);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&sSum[a]), (unsigned long long)fs[a]);
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        atomicMin(&nodes[0].st.lo[a], sLo[a]);
+        atomicMax(&nodes[0].st.hi[a], sHi[a]);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&nodes[0].st.sum[a]), (unsigned long long)sSum[a]);
+        __threadfence(); // the root's statistics are in L2 before this block counts as done
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        lastBlock = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (lastBlock && threadIdx.x == 0) {
+        __threadfence();
+        root_params(nodes, np, nt, sc, counters, terms);
+    }
+}
+
 // ---------------------------------------------------------------------------------------------------
 // Large-node phase: one persistent cooperative kernel runs every level (classify the members, grid barrier,
 // resolve and split the nodes, grid barrier). Data that other blocks write inside the kernel (member states,
@@ -579,7 +587,8 @@ __global__ void k_rr_root_params(RNode *nodes, NParam *np, int nt, const int *sc
 // ---------------------------------------------------------------------------------------------------
 struct GridBar {
     unsigned count, gen;
-    int err, pad;
+    int err;
+    unsigned ticket; // element blocks done (the last one computes the root's split)
 };
 
 // bounded wait: a barrier gives up and flags an error after this long (the levels take microseconds)
@@ -1533,11 +1542,11 @@ static void coop_cancel(int dev, int blocks)
     g_coop.cv.notify_all();
 }
 
-// Blocks of the cooperative large-node kernel: a third of what can be resident at once, no more than the
+// Blocks of the cooperative large-node kernel: a quarter of what can be resident at once, no more than the
 // members need. The two meshes of a boolean build their leaf orders concurrently, and each grid holds its SMs'
-// whole register file until it ends; the leaf order is the longer path, but the LBVH builds and the broad and
-// narrow phases run meanwhile on what is left (measured on pair_large L7, boolean step: a quarter each
-// 2.25 ms, a third 2.20 ms, a half 2.28 ms, where the candidate search is starved).
+// whole register file until it ends, while the LBVH builds and the broad and narrow phases run on what is left;
+// the share balances the two paths (measured on pair_large L7, boolean step: a third 1.76-1.80 ms, a quarter
+// 1.67 ms, a fifth 1.74 ms, a sixth 1.77 ms).
 static int top_grid(int nt, int *devOut)
 {
     static int perSm[256], sms[256];
@@ -1563,7 +1572,7 @@ static int top_grid(int nt, int *devOut)
     }
     *devOut = dev;
     const int need = (nt + kElemThreads * 4 - 1) / (kElemThreads * 4); // at least 4 members per thread
-    return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 3)));
+    return std::max(1, std::min(need, std::max(1, perSm[dev] * sms[dev] / 4)));
 }
 
 // Status of a leaf-order build from its counters and barrier record (12 ints).
@@ -1706,14 +1715,16 @@ sb_status build_reference_rank(sb_mesh *m, cudaStream_t s, bool wait)
     SB_CUDA_CHECK(cudaMemsetAsync(stamps, 0, 96 * sizeof(unsigned long long), s));
 
     const int GE = (nt + kElemThreads - 1) / kElemThreads;
+    if (!d.absMax) {
+        set_last_error("leaf order: the mesh's coordinate bound is missing");
+        return SB_ERR_INVALID;
+    }
     SB_COUNT(k_rr_init)<<<1, 1, 0, s>>>(nodes, np, nt, counters, reinterpret_cast<unsigned *>(bar));
     {
         KTime kt("k_rr_elems", s);
         SB_COUNT(k_rr_elems)<<<GE, kElemThreads, 0, s>>>(nt, d.v, d.t, d.box64, d.leafTri, rec, soa, posOf, state,
-                                                          nodes);
+                                                          nodes, np, counters, terms, scg, d.absMax, &bar->ticket);
     }
-    SB_COUNT(k_rr_root_sum)<<<GE, kElemThreads, 0, s>>>(nt, rec, soa, nodes, scg);
-    SB_COUNT(k_rr_root_params)<<<1, 1, 0, s>>>(nodes, np, nt, scg, counters, terms);
     // the large-node phase: one cooperative launch, every block resident
     if (nt > kSub) {
         int dev = 0;
