@@ -2,7 +2,7 @@
 //
 // The reference builds unit normals, per-triangle AABBs and a top-down AABB tree. Here:
 //   * per-triangle AABBs (exact FP64 min/max, plus a round-to-nearest FP32 copy for the filtered tests);
-//   * an LBVH: 30-bit Morton codes of the FP32 box centres, a radix sort, Karras' hierarchy construction
+//   * an LBVH: 24-bit Morton codes of the FP32 box centres, a radix sort, Karras' hierarchy construction
 //     (one thread per internal node) and a bottom-up refit in which the second child to arrive at a node
 //     (atomic counter) writes the union box;
 //   * unit normals are not stored: the kernels that need one recompute it with the reference's formula.
@@ -114,6 +114,13 @@ __device__ __forceinline__ uint32_t expand10(uint32_t x)
     return x;
 }
 
+// Morton code bits per axis. Eight (a 24-bit code, three radix passes instead of four for ten bits): the
+// results do not depend on the LBVH's leaf order, only the candidate search's speed does, and at 2^8 cells per
+// axis a surface mesh of a few hundred thousand triangles still holds about one or two triangles per cell
+// (equal codes are split by triangle index).
+constexpr int kMortonAxisBits = 8;
+constexpr int kMortonBits = 3 * kMortonAxisBits;
+
 __global__ void k_morton(int nt, const float *__restrict__ cen, const unsigned int *__restrict__ bounds,
                          uint32_t *__restrict__ code, int *__restrict__ idx)
 {
@@ -125,8 +132,8 @@ __global__ void k_morton(int nt, const float *__restrict__ cen, const unsigned i
         float lo = ord_to_float(bounds[a]), hi = ord_to_float(bounds[3 + a]);
         float ext = hi - lo;
         float u = ext > 0.f ? (cen[3 * (size_t)i + a] - lo) / ext : 0.f;
-        int k = (int)(u * 1024.0f);
-        q[a] = (uint32_t)min(max(k, 0), 1023);
+        int k = (int)(u * (float)(1 << kMortonAxisBits));
+        q[a] = (uint32_t)min(max(k, 0), (1 << kMortonAxisBits) - 1);
     }
     code[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
     idx[i] = i;
@@ -363,7 +370,7 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
     // temporaries: centres, bounds, unsorted keys/indices, CUB scratch
     size_t sortBytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, (uint32_t *)nullptr, (uint32_t *)nullptr, (int *)nullptr,
-                                    (int *)nullptr, nt, 0, 30, s);
+                                    (int *)nullptr, nt, 0, kMortonBits, s);
     Carve tc;
     size_t t_cen = tc.take<float>((size_t)nt * 3);
     size_t t_bnd = tc.take<unsigned int>(kBoundWords);
@@ -386,7 +393,7 @@ static sb_status prepare_begin(sb_mesh *m, int order_mode, cudaStream_t s, PrepS
     SB_COUNT(k_tri_boxes)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, d.v, d.t, d.box64, d.box32, cen, bounds);
     SB_COUNT(k_morton)<<<blocks_for(nt, BS), BS, 0, s>>>(nt, cen, bounds, keyIn, idxIn);
     SB_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(tb + t_cub, sortBytes, keyIn, d.morton, idxIn, d.leafTri, nt, 0,
-                                                  30, s));
+                                                  kMortonBits, s));
     // The reference leaf order needs only the boxes and the Morton order: it runs on a second stream while
     // this one builds and refits the LBVH.
     const bool fork = order_mode == SB_ORDER_REFERENCE;
