@@ -355,9 +355,11 @@ __global__ void k_hi32(int n, const uint64_t *__restrict__ k, int *out)
 }
 
 // Groups the intersecting pairs by cut face when one side's pairs fit one block: a block radix sort of the
-// compacted keys (face << orderBits | order, the order being the other triangle's leaf position), then the
-// runs of equal face (unique faces, their pair counts and how many there are), in one launch. Block 0 takes
-// the first mesh's faces, block 1 the second's; the pair indices land in pairIdx[side * K + i].
+// compacted keys (face << orderBits | the other triangle), then the runs of equal face (unique faces, their
+// pair counts and how many there are), in one launch. Block 0 takes the first mesh's faces, block 1 the
+// second's; the pair indices land in pairIdx[side * K + i]. With faceOnly the sort skips the low bits: the
+// pairs of each face are put in the reference's order afterwards (k_face_pair_order, by the other triangle's
+// leaf position), so only the grouping counts, and the sort takes half the passes.
 constexpr int kGroupThreads = 512;
 constexpr int kGroupItems = 16;
 constexpr int kGroupMax = kGroupThreads * kGroupItems;
@@ -370,7 +372,7 @@ union GroupSmem {
 __global__ void __launch_bounds__(kGroupThreads)
     k_face_group(int Kin, const unsigned int *dK, const uint64_t *__restrict__ keyA,
                  const uint64_t *__restrict__ keyB, const int *__restrict__ val, int orderBitsA, int orderBitsB,
-                 int endBitA, int endBitB, int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB,
+                 int endBitA, int endBitB, bool faceOnly, int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB,
                  unsigned int *runCount)
 {
     const int K = dK ? (int)*dK : Kin; // with dK, Kin bounds it (both at most kGroupMax)
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(kGroupThreads)
             v[j] = -1;
         }
     }
-    GroupSort(sm.sort).Sort(k, v, 0, endBit);
+    GroupSort(sm.sort).Sort(k, v, faceOnly ? ob : 0, endBit);
     __syncthreads(); // the sort storage is reused below
     int flags = 0;
     int prevFace = -1;
@@ -938,13 +940,15 @@ sb_status combine_impl(sb_boolean *b)
                 cudaFuncSetAttribute(k_face_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupSmem));
             });
             SB_COUNT(k_face_group)<<<2, kGroupThreads, sizeof(GroupSmem), s>>>(
-                (int)Kcap, dK, keyA, keyB, val, obA, obB, ebA, ebB, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
+                (int)Kcap, dK, keyA, keyB, val, obA, obB, ebA, ebB, useRank, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
         } else {
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, 0, 64, s);
+                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, useRank ? 32 : 0,
+                                                       64, s); // by face alone when the pair order follows
             }));
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
-                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K, 0, 64, s);
+                return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyB, keyBs, val, pairIdx + K, (int)K,
+                                                       useRank ? 32 : 0, 64, s);
             }));
             SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyAs, hiA);
             SB_COUNT(k_hi32)<<<blocks(K, 256), 256, 0, s>>>((int)K, keyBs, hiB);
