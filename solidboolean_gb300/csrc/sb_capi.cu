@@ -375,7 +375,12 @@ __global__ void __launch_bounds__(kGroupThreads)
                  int endBitA, int endBitB, bool faceOnly, int *pairIdx, int *uqA, int *ctA, int *uqB, int *ctB,
                  unsigned int *runCount)
 {
-    const int K = dK ? (int)*dK : Kin; // with dK, Kin bounds it (both at most kGroupMax)
+    const int K = dK ? (int)*dK : Kin; // with dK, Kin bounds it
+    if (K > kGroupMax) { // beyond one block: the host groups them device-wide once it has read the count
+        if (threadIdx.x == 0)
+            runCount[blockIdx.x] = 0;
+        return;
+    }
     extern __shared__ __align__(16) unsigned char smemRaw[];
     GroupSmem &sm = *reinterpret_cast<GroupSmem *>(smemRaw);
     __shared__ int warpSums[kGroupThreads / 32];
@@ -873,10 +878,12 @@ sb_status combine_impl(sb_boolean *b)
             return cub::DeviceSelect::Flagged(tmp, bytes, thrust::counting_iterator<int>(0), hit, sel,
                                               d_count + 1, (int)C, s);
         }));
-    // With few candidates the intersecting pairs fit the one-block grouping whatever their number: their count
-    // stays on the device until the faces are counted, which saves a host round trip on small booleans.
+    // The count of intersecting pairs stays on the device until the faces are counted (a host round trip
+    // fewer), the candidate count bounding the buffers it would size: the one-block grouping takes the count
+    // from the device, and only a count beyond its reach is grouped device-wide once read.
+    constexpr unsigned int kDeferMax = 1u << 20;
     unsigned int K = 0;
-    const bool deferK = C > 0 && C <= (unsigned int)kGroupMax;
+    const bool deferK = C > 0 && C <= kDeferMax;
     if (C > 0 && !deferK) {
         sb_status r = read_back(b, &K, d_count + 1, sizeof K);
         if (r != SB_OK)
@@ -932,16 +939,8 @@ sb_status combine_impl(sb_boolean *b)
     if (Kcap > 0) {
         SB_COUNT(k_pair_keys)<<<blocks(Kcap, 256), 256, 0, s>>>((int)Kcap, dK, sel, candSorted, nB, nullptr, nullptr,
                                                       seg, perm, keyA, keyB, val, segK, pairAB, pairPerm);
-        if (Kcap <= (unsigned int)kGroupMax) {
-            const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
-            const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
-            static std::once_flag smemOnce;
-            std::call_once(smemOnce, [] {
-                cudaFuncSetAttribute(k_face_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupSmem));
-            });
-            SB_COUNT(k_face_group)<<<2, kGroupThreads, sizeof(GroupSmem), s>>>(
-                (int)Kcap, dK, keyA, keyB, val, obA, obB, ebA, ebB, useRank, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
-        } else {
+        // device-wide grouping (the count K known on the host)
+        auto groupDeviceWide = [&]() -> sb_status {
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
                 return cub::DeviceRadixSort::SortPairs(tmp, bytes, keyA, keyAs, val, pairIdx, (int)K, useRank ? 32 : 0,
                                                        64, s); // by face alone when the pair order follows
@@ -958,13 +957,38 @@ sb_status combine_impl(sb_boolean *b)
             SB_CUDA_CHECK(cub_run(b, [&](void *tmp, size_t &bytes) {
                 return cub::DeviceRunLengthEncode::Encode(tmp, bytes, hiB, uqB, ctB, d_count + 3, (int)K, s);
             }));
+            return SB_OK;
+        };
+        if (deferK || Kcap <= (unsigned int)kGroupMax) {
+            const int obA = end_bit_for((uint64_t)std::max(nB, 1)), obB = end_bit_for((uint64_t)std::max(nA, 1));
+            const int ebA = obA + end_bit_for((uint64_t)std::max(nA, 1)), ebB = obB + end_bit_for((uint64_t)std::max(nB, 1));
+            static std::once_flag smemOnce;
+            std::call_once(smemOnce, [] {
+                cudaFuncSetAttribute(k_face_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupSmem));
+            });
+            SB_COUNT(k_face_group)<<<2, kGroupThreads, sizeof(GroupSmem), s>>>(
+                (int)Kcap, dK, keyA, keyB, val, obA, obB, ebA, ebB, useRank, pairIdx, uqA, ctA, uqB, ctB, d_count + 2);
+        } else {
+            const sb_status r = groupDeviceWide();
+            if (r != SB_OK)
+                return r;
         }
         unsigned int runs[2];
-        Readback rb(b);
-        SB_CUDA_CHECK(rb.add(runs, d_count + 2, sizeof runs));
-        if (deferK)
-            SB_CUDA_CHECK(rb.add(&K, d_count + 1, sizeof K));
-        SB_CUDA_CHECK(rb.sync());
+        {
+            Readback rb(b);
+            SB_CUDA_CHECK(rb.add(runs, d_count + 2, sizeof runs));
+            if (deferK)
+                SB_CUDA_CHECK(rb.add(&K, d_count + 1, sizeof K));
+            SB_CUDA_CHECK(rb.sync());
+        }
+        if (deferK && K > (unsigned int)kGroupMax) { // the one-block grouping left them
+            const sb_status r = groupDeviceWide();
+            if (r != SB_OK)
+                return r;
+            Readback rb(b);
+            SB_CUDA_CHECK(rb.add(runs, d_count + 2, sizeof runs));
+            SB_CUDA_CHECK(rb.sync());
+        }
         FA = (int)runs[0];
         FB = (int)runs[1];
     }
