@@ -81,6 +81,9 @@ typedef struct sb_options {
     int32_t order;       /* sb_order */
     void *stream;        /* cudaStream_t */
     uint32_t robust;     /* sb_robust flags; 0 (default) = the reference's behaviour */
+    uint32_t stage_results; /* 1: sb_combine also copies the result vertices and the three fetch results to
+                               page-locked host memory (see sb_take_staged); 0 (default): results stay on the
+                               device until sb_fetch / sb_result_vertices copy them */
 } sb_options;
 
 typedef struct sb_stats {
@@ -223,6 +226,17 @@ void sb_batch_destroy(sb_batch *b);
  * SB_ERR_CUDA when no page-locked memory can be had; sb_host_free(NULL) does nothing. Thread-safe. */
 sb_status sb_host_alloc(size_t bytes, void **ptr);
 void sb_host_free(void *ptr);
+
+/* No counterpart in the reference. With sb_options.stage_results set, sb_combine copies the result vertices
+ * to page-locked host memory as soon as the weld has numbered them (on a copy stream, beside the rest of the
+ * combine) and the three fetch results once their sizes are known, and returns with all four on the host.
+ * sb_take_staged hands one of them over: what = SB_UNION, SB_DIFF or SB_INTERSECT (uint32 index triplets) or
+ * SB_STAGED_VERTICES (FP64 xyz triplets); *count = its rows. The caller owns *host afterwards and releases it
+ * with sb_host_free. *host is NULL when nothing is staged (staging off, already taken, zero rows, or no
+ * page-locked memory): sb_fetch / sb_result_vertices still copy from the device. Buffers not taken are
+ * released by the next combine and by sb_boolean_destroy. */
+#define SB_STAGED_VERTICES 3
+sb_status sb_take_staged(sb_boolean *b, int32_t what, void **host, size_t *count);
 
 #ifdef __cplusplus
 }

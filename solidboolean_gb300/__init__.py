@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libsolidboolean_gb300.so")
 SB_OK, SB_FAIL_ATTACH, SB_FAIL_LINK, SB_FAIL_LOOP = 0, 1, 2, 3
 SB_ERR_INVALID, SB_ERR_CUDA, SB_ERR_CAPACITY, SB_ERR_NOT_COMBINED = 10, 11, 12, 13
 SB_UNION, SB_DIFF, SB_INTERSECT = 0, 1, 2
+SB_STAGED_VERTICES = 3  # sb_take_staged: the result vertices
 PRECISION = {"filtered": 0, "fp64": 1}
 ORDER = {"reference": 0, "index": 1}
 # sb_robust flags (include/solidboolean_gb300.h): 0 keeps the reference's behaviour
@@ -35,12 +36,12 @@ EXPORTS = ["sb_default_options", "sb_status_string", "sb_last_error", "sb_kernel
            "sb_mesh_create_device",
            "sb_mesh_update_vertices_device", "sb_mesh_prepare", "sb_mesh_destroy", "sb_boolean_create",
            "sb_combine", "sb_fetch", "sb_result_vertices", "sb_fetch_device", "sb_result_vertices_device",
-           "sb_debug_dump", "sb_boolean_destroy", "sb_host_alloc", "sb_host_free"]
+           "sb_debug_dump", "sb_boolean_destroy", "sb_host_alloc", "sb_host_free", "sb_take_staged"]
 
 
 class Options(ctypes.Structure):
     _fields_ = [("weld_factor", ctypes.c_int64), ("precision", ctypes.c_int32), ("order", ctypes.c_int32),
-                ("stream", ctypes.c_void_p), ("robust", ctypes.c_uint32)]
+                ("stream", ctypes.c_void_p), ("robust", ctypes.c_uint32), ("stage_results", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -115,6 +116,8 @@ def lib() -> ctypes.CDLL:
     L.sb_host_alloc.argtypes = [sz, ctypes.POINTER(vp)]
     L.sb_host_free.restype = None
     L.sb_host_free.argtypes = [vp]
+    L.sb_take_staged.restype = st
+    L.sb_take_staged.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(vp), ctypes.POINTER(sz)]
     L.sb_adjoint.restype = st
     L.sb_adjoint.argtypes = [vp, vp, vp, vp, vp]
     _lib = L
@@ -133,7 +136,7 @@ def _check(code: int, what: str) -> int:
 
 
 def make_options(weld_factor: int = 100000, precision: str = "filtered", order: str = "reference",
-                 stream: int | None = None, robust: int = 0) -> Options:
+                 stream: int | None = None, robust: int = 0, stage_results: bool = False) -> Options:
     o = Options()
     lib().sb_default_options(ctypes.byref(o))
     o.weld_factor = int(weld_factor)
@@ -141,6 +144,7 @@ def make_options(weld_factor: int = 100000, precision: str = "filtered", order: 
     o.order = ORDER[order]
     o.stream = stream or None
     o.robust = int(robust)
+    o.stage_results = 1 if stage_results else 0
     return o
 
 
@@ -211,7 +215,9 @@ class SolidBoolean:
 
     def __init__(self, first: SolidMesh, second: SolidMesh, options: Options | None = None):
         self.first, self.second = first, second
-        self.options = options or make_options()
+        # results are read on the host here: combine() stages them in page-locked memory (sb_take_staged)
+        self.options = Options.from_buffer_copy(options) if options is not None else make_options()
+        self.options.stage_results = 1
         self._h = ctypes.c_void_p()
         self.status = None
         self.stats = Stats()
@@ -226,7 +232,26 @@ class SolidBoolean:
         self.status = _check(lib().sb_combine(self._handle(), ctypes.byref(self.stats)), "sb_combine")
         return self.status == SB_OK
 
+    def _take_staged(self, what: int, cols: int, dtype) -> np.ndarray | None:
+        """The result combine() staged in page-locked host memory, handed over (None when not staged)."""
+        L = lib()
+        ptr, n = ctypes.c_void_p(), ctypes.c_size_t()
+        _check(L.sb_take_staged(self._handle(), what, ctypes.byref(ptr), ctypes.byref(n)), "sb_take_staged")
+        if n.value == 0:
+            if ptr.value:
+                L.sb_host_free(ptr.value)
+            return np.zeros((0, cols), dtype=dtype)
+        if not ptr.value:
+            return None
+        nbytes = n.value * cols * np.dtype(dtype).itemsize
+        raw = (ctypes.c_char * nbytes).from_address(ptr.value)
+        weakref.finalize(raw, L.sb_host_free, ptr.value)
+        return np.frombuffer(raw, dtype=dtype).reshape(n.value, cols)
+
     def _fetch(self, op: int) -> np.ndarray:
+        staged = self._take_staged(op, 3, np.uint32)
+        if staged is not None:
+            return staged
         L = lib()
         n = ctypes.c_size_t()
         _check(L.sb_fetch(self._handle(), op, None, 0, ctypes.byref(n)), "sb_fetch")
@@ -248,6 +273,9 @@ class SolidBoolean:
         resultTriangles.extend(self._fetch(SB_INTERSECT).tolist())
 
     def resultVertices(self) -> np.ndarray:
+        staged = self._take_staged(SB_STAGED_VERTICES, 3, np.float64)
+        if staged is not None:
+            return staged
         L = lib()
         n = ctypes.c_size_t()
         _check(L.sb_result_vertices(self._handle(), None, 0, ctypes.byref(n)), "sb_result_vertices")

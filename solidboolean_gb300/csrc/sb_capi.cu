@@ -681,11 +681,38 @@ struct sb_boolean {
     cudaEvent_t retriDone = nullptr; // the re-triangulated triangles' numbering, computed on `side`
     bool evInit = false;
     char *mail = nullptr; // pinned mailbox: small reads [0, kMailRead), constant uploads after it
+    // results staged in page-locked host memory (sb_options.stage_results): the three fetches, the vertices
+    struct Staged {
+        void *ptr = nullptr;
+        size_t count = 0;
+    } staged[4];
+    cudaStream_t stage = nullptr; // copy stream of the vertex staging
+    cudaEvent_t stageEv = nullptr;
+    bool staging = false;         // a copy to the host is in flight on `stage`
 };
 
 constexpr size_t kMailRead = kMailBytes - 64;
 
 namespace {
+
+// waits for the vertex staging copy, if one is in flight
+cudaError_t staged_wait(sb_boolean *b)
+{
+    if (!b->staging)
+        return cudaSuccess;
+    b->staging = false;
+    return cudaStreamSynchronize(b->stage);
+}
+
+// releases the staged buffers nobody took
+void staged_release(sb_boolean *b)
+{
+    for (auto &x : b->staged) {
+        if (x.ptr)
+            sb_host_free(x.ptr);
+        x = sb_boolean::Staged{};
+    }
+}
 
 template <class F> sb_status guarded(F &&f)
 {
@@ -779,6 +806,8 @@ sb_status combine_impl(sb_boolean *b)
     sb_stats &st = b->stats;
     std::memset(&st, 0, sizeof st);
     b->combined = false;
+    SB_CUDA_CHECK(staged_wait(b));
+    staged_release(b);
     for (int k = 0; k < 3; ++k) {
         b->d_fetch[k] = nullptr;
         b->nFetch[k] = 0;
@@ -1387,6 +1416,21 @@ sb_status combine_impl(sb_boolean *b)
         SB_CUDA_CHECK(
             cudaMemcpyAsync(g.newV + 3 * (size_t)A.nv, B.v, sizeof(double) * 3 * B.nv, cudaMemcpyDeviceToDevice, s));
     launch_weld_number(g, (int)nSeq, s);
+    if (b->opts.stage_results && nV > 0) {
+        // the result vertices are final: copied to the host on the copy stream beside the rest
+        if (!b->stage) {
+            SB_CUDA_CHECK(cudaStreamCreateWithFlags(&b->stage, cudaStreamNonBlocking));
+            SB_CUDA_CHECK(cudaEventCreateWithFlags(&b->stageEv, cudaEventDisableTiming));
+        }
+        void *hv = nullptr;
+        if (sb_host_alloc(sizeof(double) * 3 * nV, &hv) == SB_OK && hv) {
+            b->staged[SB_STAGED_VERTICES] = sb_boolean::Staged{hv, nV};
+            SB_CUDA_CHECK(cudaEventRecord(b->stageEv, s));
+            SB_CUDA_CHECK(cudaStreamWaitEvent(b->stage, b->stageEv, 0));
+            b->staging = true;
+            SB_CUDA_CHECK(cudaMemcpyAsync(hv, g.newV, sizeof(double) * 3 * nV, cudaMemcpyDeviceToHost, b->stage));
+        }
+    }
     if (nTri > 0)
         SB_COUNT(k_tri_mesh)<<<blocks(nTri, 256), 256, 0, s>>>(nTri, cnts[0], cnts[1], cnts[2], g.triMesh, g.isUncut);
     launch_arrangement(g, s);
@@ -1643,6 +1687,19 @@ sb_status combine_impl(sb_boolean *b)
         cudaEventElapsedTime(&ms, b->ev[k], b->ev[k + 1]);
         st.stage_ms[k] = ms;
     }
+    if (b->opts.stage_results && status == SB_OK) {
+        // the three fetch results, sized now, in one more round trip; the vertices' copy ended long ago
+        for (int op = 0; op < 3; ++op) {
+            const size_t n = b->nFetch[op];
+            void *h = nullptr;
+            if (n && sb_host_alloc(sizeof(uint32_t) * 3 * n, &h) == SB_OK && h) {
+                b->staged[op] = sb_boolean::Staged{h, n};
+                SB_CUDA_CHECK(cudaMemcpyAsync(h, b->d_fetch[op], sizeof(uint32_t) * 3 * n, cudaMemcpyDeviceToHost, s));
+            }
+        }
+        SB_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    SB_CUDA_CHECK(staged_wait(b));
     b->status = status;
     b->combined = true;
     return status;
@@ -1664,6 +1721,7 @@ void sb_default_options(sb_options *o)
     o->order = SB_ORDER_REFERENCE;
     o->stream = nullptr;
     o->robust = 0;
+    o->stage_results = 0;
 }
 
 const char *sb_status_string(sb_status s)
@@ -2031,6 +2089,19 @@ sb_status sb_fetch(sb_boolean *b, sb_op op, uint32_t *tris, size_t cap, size_t *
     return SB_OK;
 }
 
+sb_status sb_take_staged(sb_boolean *b, int32_t what, void **host, size_t *count)
+{
+    sb_status r = check_fetchable(b);
+    if (r != SB_OK)
+        return r;
+    if (what < SB_UNION || what > SB_STAGED_VERTICES || !host || !count)
+        return SB_ERR_INVALID;
+    *count = what == SB_STAGED_VERTICES ? b->nNewV : (b->status == SB_OK ? b->nFetch[what] : 0);
+    *host = b->staged[what].ptr;
+    b->staged[what] = sb_boolean::Staged{};
+    return SB_OK;
+}
+
 sb_status sb_fetch_device(sb_boolean *b, sb_op op, const uint32_t **d_tris, size_t *count)
 {
     sb_status r = check_fetchable(b);
@@ -2159,6 +2230,12 @@ void sb_boolean_destroy(sb_boolean *b)
     if (b->side) {
         cudaStreamDestroy(b->side);
         cudaEventDestroy(b->sideDone);
+    }
+    staged_wait(b);
+    staged_release(b);
+    if (b->stage) {
+        cudaStreamDestroy(b->stage);
+        cudaEventDestroy(b->stageEv);
     }
     pinned_mail_release(b->mail);
     delete b;
@@ -2293,6 +2370,7 @@ sb_status sb_batch_combine(size_t n, const double *xyz_a, const uint64_t *v_off_
                     st = mesh_alloc(0, 0, &k.mb);
                 sb_options o = base;
                 o.stream = k.s;
+                o.stage_results = 0; // the batch copies the results it keeps itself
                 if (st == SB_OK)
                     st = sb_boolean_create(k.ma, k.mb, &o, &k.x);
                 if (st == SB_OK && !stageFor(inMax))
