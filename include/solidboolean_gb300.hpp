@@ -55,27 +55,50 @@ private:
 
 template <class Vector3> class SolidBoolean {
 public:
+    // The results are read on the host through this class, so combine() stages them in page-locked memory
+    // (sb_options.stage_results): the reads below convert from there instead of copying from the device.
     SolidBoolean(const SolidMesh<Vector3> *firstMesh, const SolidMesh<Vector3> *secondMesh,
                  const sb_options *opts = nullptr)
     {
-        SolidMesh<Vector3>::check(sb_boolean_create(firstMesh->handle(), secondMesh->handle(), opts, &m_b));
+        sb_options o;
+        if (opts)
+            o = *opts;
+        else
+            sb_default_options(&o);
+        o.stage_results = 1;
+        SolidMesh<Vector3>::check(sb_boolean_create(firstMesh->handle(), secondMesh->handle(), &o, &m_b));
     }
     ~SolidBoolean() { sb_boolean_destroy(m_b); }
-    bool combine() { return sb_combine(m_b, nullptr) == SB_OK; }
+    bool combine()
+    {
+        m_haveVertices = false;
+        return sb_combine(m_b, nullptr) == SB_OK;
+    }
     void fetchUnion(std::vector<std::vector<size_t>> &out) { fetch(SB_UNION, out); }
     void fetchDiff(std::vector<std::vector<size_t>> &out) { fetch(SB_DIFF, out); }
     void fetchIntersect(std::vector<std::vector<size_t>> &out) { fetch(SB_INTERSECT, out); }
+    // built once per combine, like the reference's member (src/solidboolean.h:44)
     const std::vector<Vector3> &resultVertices()
     {
-        size_t n = 0;
-        m_resultVertices.clear();
-        if (sb_result_vertices(m_b, nullptr, 0, &n) != SB_OK)
+        if (m_haveVertices)
             return m_resultVertices;
-        std::vector<double> xyz(3 * n);
-        SolidMesh<Vector3>::check(sb_result_vertices(m_b, xyz.data(), n, &n));
+        m_resultVertices.clear();
+        size_t n = 0;
+        void *staged = nullptr;
+        if (sb_take_staged(m_b, SB_STAGED_VERTICES, &staged, &n) != SB_OK)
+            return m_resultVertices;
+        std::vector<double> copy;
+        const double *xyz = static_cast<const double *>(staged);
+        if (!staged && n) {
+            copy.resize(3 * n);
+            SolidMesh<Vector3>::check(sb_result_vertices(m_b, copy.data(), n, &n));
+            xyz = copy.data();
+        }
         m_resultVertices.reserve(n);
         for (size_t i = 0; i < n; ++i)
             m_resultVertices.emplace_back(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+        sb_host_free(staged);
+        m_haveVertices = true;
         return m_resultVertices;
     }
 
@@ -84,15 +107,26 @@ private:
     void fetch(sb_op op, std::vector<std::vector<size_t>> &out)
     {
         size_t n = 0;
-        if (sb_fetch(m_b, op, nullptr, 0, &n) != SB_OK || n == 0)
+        void *staged = nullptr;
+        if (sb_take_staged(m_b, op, &staged, &n) != SB_OK || n == 0) {
+            sb_host_free(staged);
             return;
-        std::vector<uint32_t> t(3 * n);
-        SolidMesh<Vector3>::check(sb_fetch(m_b, op, t.data(), n, &n));
+        }
+        std::vector<uint32_t> copy;
+        const uint32_t *t = static_cast<const uint32_t *>(staged);
+        if (!staged) {
+            copy.resize(3 * n);
+            SolidMesh<Vector3>::check(sb_fetch(m_b, op, copy.data(), n, &n));
+            t = copy.data();
+        }
+        out.reserve(out.size() + n);
         for (size_t i = 0; i < n; ++i)
             out.push_back({t[3 * i], t[3 * i + 1], t[3 * i + 2]});
+        sb_host_free(staged);
     }
     sb_boolean *m_b = nullptr;
     std::vector<Vector3> m_resultVertices;
+    bool m_haveVertices = false;
 };
 
 } // namespace solidboolean_gb300
