@@ -1848,11 +1848,15 @@ sb_status sb_mesh_create(const double *xyz, size_t nv, const uint32_t *tris, siz
         if (r != SB_OK)
             return r;
         sb_mesh *m = *out;
+        // both uploads and the index check in stream order, one host round trip (the check's read-back waits
+        // for the copies, so the caller's arrays are free again when this returns)
         if (nv)
-            SB_CUDA_CHECK(cudaMemcpy(m->d.v, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice));
+            SB_CUDA_CHECK(cudaMemcpyAsync(m->d.v, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, nullptr));
         if (nt)
-            SB_CUDA_CHECK(cudaMemcpy(m->d.t, tris, sizeof(uint32_t) * 3 * nt, cudaMemcpyHostToDevice));
+            SB_CUDA_CHECK(cudaMemcpyAsync(m->d.t, tris, sizeof(uint32_t) * 3 * nt, cudaMemcpyHostToDevice, nullptr));
         r = mesh_validate(m, nullptr);
+        if (r == SB_OK && nt == 0 && nv)
+            SB_CUDA_CHECK(cudaStreamSynchronize(nullptr)); // no check ran: wait for the vertex copy
         if (r != SB_OK) {
             sb_mesh_destroy(m);
             *out = nullptr;
